@@ -1,0 +1,212 @@
+/*
+ * ktruss_gb300.h — C ABI of libktruss_gb300, a GB300 (sm_103a) k-truss engine that drops in
+ * for KTrussExplorer's k-truss path.
+ *
+ * Every entry point takes plain pointers and sizes and returns an int status (kt_status).
+ * The last error message of the calling thread is available from kt_last_error().
+ *
+ * Reference interfaces replaced (paths are inside the ktruss-explorer project):
+ *   kt_ktruss            <- void ktruss(COOGraph* graph, COOGraph* truss, Config config)
+ *                           kernel.h:12, kernel.cu:9-39 (dispatch, relabel, GPU/CPU drivers)
+ *   kt_verify            <- void verify(COOGraph* graph, Config config)         verify.cu:12-40
+ *   kt_read_tsv          <- COOGraph* createCOOFromFile(const char* fileName)  graph.cu:37-79
+ *   kt_write_tsv         <- void writeCOOGraphToFile(COOGraph*, const char*)   graph.cu:96-104
+ *   kt_coo_alloc/free    <- createEmptyCOO / freeCOOGraph                       graph.cu:10-18, 81-85
+ *   kt_config_default,
+ *   kt_parse_args        <- Config parseArgs(int, char**)                       config.h:183-224
+ *   kt_print_config,
+ *   kt_print_config_csv  <- printConfig / printConfigAsCSV                      config.h:226-272
+ * New (no counterpart in the reference, which computes one k per run):
+ *   kt_decompose         per-edge truss numbers and k_max in one call (the reference obtains
+ *                        them only by chaining ktruss() over k = 3, 4, ...)
+ *   kt_engine_*          device-resident engine: persistent workspace, caller-owned device
+ *                        buffers, one CUDA stream
+ *   kt_gen_*             seeded synthetic graph generators
+ */
+#ifndef KTRUSS_GB300_H
+#define KTRUSS_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes -------------------------------------------------------------------- */
+/* The reference reports errors by assert() or exit(0); each assert becomes a status here. */
+typedef enum kt_status {
+    KT_OK = 0,
+    KT_ERR_INVALID_ARG = 1,     /* null pointer, bad enum value, bad size                     */
+    KT_ERR_SELF_LOOP = 2,       /* graph.cu:54 "Edges from a vertex to itself are not allowed" */
+    KT_ERR_NOT_SYMMETRIC = 3,   /* an entry (u,v) without its reverse (v,u), or a duplicate    */
+    KT_ERR_CAPACITY = 4,        /* output capacity below the edge count (graph.cu:111,122)     */
+    KT_ERR_UNSUPPORTED = 5,     /* processor=cpu: this library implements the GPU path only    */
+    KT_ERR_CUDA = 6,            /* a CUDA runtime call failed                                   */
+    KT_ERR_DEVICE_ALLOC = 7,    /* device memory exhausted                                     */
+    KT_ERR_HOST_ALLOC = 8,
+    KT_ERR_IO = 9,              /* file cannot be opened or parsed (graph.cu:47,52-53)          */
+    KT_ERR_MISMATCH = 10,       /* verify: edge count or edge set differs (verify.cu:18,28-29)  */
+    KT_ERR_TIMEOUT = 11,        /* a bounded device-side wait expired; the device stays usable */
+    KT_ERR_NO_DEVICE = 12,
+    KT_ERR_TOO_LARGE = 13       /* graph exceeds the 32-bit index space of the layout          */
+} kt_status;
+
+/* ---- graph and configuration structs -------------------------------------------------- */
+
+/* Same field order and types as COOGraph (graph.h:10-16).  An undirected graph stores each
+ * edge twice, once per direction; num_edges counts both.  Vertex ids are 0-based. */
+typedef struct kt_coo {
+    uint32_t num_nodes;
+    uint32_t num_edges;
+    uint32_t capacity;
+    uint32_t* src_idx;
+    uint32_t* dst_idx;
+} kt_coo;
+
+/* Enum values of config.h:51-161. */
+enum { KT_PROCESSOR_CPU = 0, KT_PROCESSOR_GPU = 1 };
+enum { KT_UNDIRECTED = 0, KT_DIRECTED_BY_INDEX = 1, KT_DIRECTED_BY_DEGREE = 2 };
+enum { KT_FORMAT_COOCSR = 0, KT_FORMAT_TILED_COOCSR = 1 };
+enum { KT_RECOUNT_ALL = 0, KT_RECOUNT_AFFECTED = 1 };
+
+/* Same field order as Config (config.h:163-181); the four enums are int32. */
+typedef struct kt_config {
+    const char* graph_file_name;
+    uint32_t k;
+    const char* compare_file_name;
+    const char* out_file_name;
+    uint32_t num_warmup_runs;
+    uint32_t num_timed_runs;
+    int32_t processor;
+    int32_t directedness;
+    int32_t input_format;
+    uint32_t num_edge_remove_iter;
+    int32_t recount;
+    uint32_t block_size;
+    uint32_t num_tiles;
+    uint32_t num_parallel_tiles;
+    uint32_t verbosity;
+    uint32_t num_nodes; /* filled from the graph by the caller, as main.cu:23-24 does */
+    uint32_t num_edges;
+} kt_config;
+
+/* Canonical undirected edge list (u < v, sorted, no duplicates), returned by generators. */
+typedef struct kt_edges {
+    uint32_t num_nodes;
+    uint64_t num_edges;
+    uint32_t* u;
+    uint32_t* v;
+} kt_edges;
+
+/* ---- errors ---------------------------------------------------------------------------- */
+const char* kt_last_error(void);
+const char* kt_status_string(int status);
+
+/* ---- configuration (config.h) --------------------------------------------------------- */
+/* Defaults of parseArgs (config.h:184-199). */
+void kt_config_default(kt_config* config);
+/* getopt string "g:k:o:w:x:c:p:d:f:e:r:b:t:y:v:h" (config.h:201).  Returns KT_OK, or
+ * KT_ERR_INVALID_ARG for an unknown option or enum value (the reference exits with status 0
+ * there, config.h:62-63).  -h prints the usage text and returns KT_ERR_INVALID_ARG too. */
+int kt_parse_args(int argc, char** argv, kt_config* config);
+void kt_print_usage(void);
+void kt_print_config(const kt_config* config);
+void kt_print_config_csv(const kt_config* config);
+
+/* ---- graph I/O (graph.cu) ------------------------------------------------------------- */
+/* Allocates host arrays of `capacity` entries; num_edges = 0. */
+int kt_coo_alloc(uint32_t num_nodes, uint32_t capacity, kt_coo* out);
+void kt_coo_free(kt_coo* graph);
+/* Reads "dst src x" lines, 1-based ids (graph.cu:51-62); num_nodes = largest id seen. */
+int kt_read_tsv(const char* path, kt_coo* out);
+/* Writes "dst+1 \t src+1 \t 1" per entry (graph.cu:96-104). */
+int kt_write_tsv(const kt_coo* graph, const char* path);
+/* Decomposition output: "dst+1 \t src+1 \t t(e)" per entry; readers of the reference format
+ * ignore the third column (graph.cu:53). */
+int kt_write_truss_tsv(const kt_coo* graph, const uint32_t* truss_per_entry, const char* path);
+
+/* ---- the k-truss path ----------------------------------------------------------------- */
+/* k-truss of `graph` for config->k (kernel.h:12).  `graph` holds a symmetric simple graph
+ * (both directions, no self loops, no duplicates).  On return `truss` holds the edges of the
+ * k-truss in both directions with the input's vertex ids, in unspecified order, and
+ * truss->num_nodes = graph->num_nodes.  truss->capacity must be >= graph->num_edges.
+ * Semantics follow the reference: k = 2 keeps every edge; k < 2 keeps none (k-2 wraps as an
+ * unsigned value).  config->directedness, input_format, recount, num_edge_remove_iter,
+ * block_size, num_tiles and num_parallel_tiles select the GPU schedule; the edge set returned
+ * does not depend on them.  num_warmup_runs/num_timed_runs repeat the computation and, at
+ * verbosity 0, print the config.h:247-272 CSV line with the time of each timed run.
+ * Unlike the reference, `graph` is not relabeled in place.  processor = CPU returns
+ * KT_ERR_UNSUPPORTED. */
+int kt_ktruss(const kt_coo* graph, kt_coo* truss, const kt_config* config);
+
+/* Full decomposition: truss_per_entry[i] = t(e) of the edge of entry i (same value for both
+ * directions), where t(e) = max k such that e is in the k-truss (>= 2).  *k_max = max t(e)
+ * (0 for a graph without edges).  config may be NULL (defaults). */
+int kt_decompose(const kt_coo* graph, uint32_t* truss_per_entry, uint32_t* k_max,
+                 const kt_config* config);
+
+/* verify.cu:12-40: reads config->compare_file_name and compares edge sets (order-insensitive).
+ * Returns KT_ERR_MISMATCH instead of aborting; prints "    PASSED" at verbosity >= 1. */
+int kt_verify(const kt_coo* truss, const kt_config* config);
+
+/* ---- device-resident engine ----------------------------------------------------------- */
+typedef struct kt_engine kt_engine;
+
+/* Statistics of the last engine call (filled by kt_engine_stats). */
+typedef struct kt_stats {
+    uint32_t num_nodes;          /* vertices of the built graph                              */
+    uint64_t num_edges;          /* undirected edges m (= oriented edges E+)                 */
+    uint32_t k_max;
+    uint32_t num_levels;         /* peel levels that removed at least one edge               */
+    uint32_t num_rounds;         /* peel rounds (frontier batches) executed                  */
+    uint64_t triangles;          /* triangles of the input graph                             */
+    uint64_t plain_alive_sum;    /* sum over the passes of the reference's full-recount
+                                    schedule of the alive oriented edges E+_p                  */
+    uint32_t plain_passes;       /* number of such passes                                    */
+    uint64_t kernel_launches;    /* kernels launched by the engine since creation            */
+    float last_ms;               /* device time of the last call (CUDA events)               */
+    float build_ms;              /* of which: device CSR build (relabel, sort, orient)        */
+    float support_ms;            /*           support count                                   */
+    float peel_ms;               /*           peeling and output                              */
+} kt_stats;
+
+/* Creates an engine on `device` with its own non-blocking CUDA stream. */
+int kt_engine_create(int device, kt_engine** out);
+int kt_engine_destroy(kt_engine* engine);
+/* Returns the engine's cudaStream_t (as void*). */
+void* kt_engine_stream(kt_engine* engine);
+/* Pre-allocates the device workspace for graphs up to these sizes, so that later calls of at
+ * most this size do not allocate. */
+int kt_engine_reserve(kt_engine* engine, uint32_t max_nodes, uint64_t max_entries);
+/* Device-resident decomposition.  d_src/d_dst: num_entries entries on the engine's device
+ * (symmetric simple graph, both directions).  d_truss_per_entry: num_entries outputs.
+ * d_k_max: one uint32 on the device.  Work is enqueued on the engine stream; the call
+ * returns once it is enqueued unless `sync` is nonzero. */
+int kt_engine_decompose(kt_engine* engine, const uint32_t* d_src, const uint32_t* d_dst,
+                        uint64_t num_entries, uint32_t num_nodes, uint32_t* d_truss_per_entry,
+                        uint32_t* d_k_max, int sync);
+/* Device-resident single-k truss: d_keep[i] = 1 if entry i's edge is in the k-truss, else 0. */
+int kt_engine_ktruss(kt_engine* engine, const uint32_t* d_src, const uint32_t* d_dst,
+                     uint64_t num_entries, uint32_t num_nodes, uint32_t k, uint8_t* d_keep,
+                     int sync);
+/* Synchronizes the engine stream and fills *stats. */
+int kt_engine_stats(kt_engine* engine, kt_stats* stats);
+
+/* ---- seeded generators (no counterpart in the reference, which ships no data) --------- */
+int kt_gen_rmat(uint32_t scale, uint32_t edge_factor, double a, double b, double c,
+                uint64_t seed, kt_edges* out);
+int kt_gen_er(uint32_t n, double p, uint64_t seed, kt_edges* out);
+int kt_gen_ba(uint32_t n, uint32_t m, uint64_t seed, kt_edges* out);
+int kt_gen_ws(uint32_t n, uint32_t k, double p, uint64_t seed, kt_edges* out);
+int kt_gen_rgg(uint32_t n, double radius, uint64_t seed, kt_edges* out);
+/* Adds `count` cliques of min_size..max_size random distinct vertices to the edge list
+ * (u[i], v[i]) of a graph with num_nodes vertices; the result is canonical again. */
+int kt_plant_cliques(uint32_t num_nodes, const uint32_t* u, const uint32_t* v, uint64_t num_edges,
+                     uint32_t count, uint32_t min_size, uint32_t max_size, uint64_t seed, kt_edges* out);
+void kt_edges_free(kt_edges* graph);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* KTRUSS_GB300_H */

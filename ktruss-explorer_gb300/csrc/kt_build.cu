@@ -1,0 +1,268 @@
+// Device-side graph build: the GB300 replacement for the reference's relabel and COO->CSR
+// conversion (sortByDegree graph.cu:152-185, undirected2directedCOO graph.cu:194-237,
+// coo2coocsrOnDevice graph.cu:435-478).  The reference sorts vertices on the CPU and sorts
+// every adjacency list on the CPU between two PCIe copies; here everything stays in HBM:
+//
+//   1. degree histogram of the input entries (with id, self-loop checks);
+//   2. vertex rank = position in ascending (degree, id) order (radix sort of n keys);
+//   3. every entry becomes the key (rank[src] << vb | rank[dst]) carrying its entry index;
+//      one radix sort of the 2m keys yields the symmetric CSR with rows sorted by rank;
+//   4. each row splits at its own rank: the part above it is the row of the degree-oriented
+//      CSR (edge id = position in the oriented array); the part below gets its edge id by a
+//      binary search in the neighbour's oriented row, which also proves the input symmetric.
+//
+// Layout in HBM (n vertices, m undirected edges, all uint32):
+//   s_ptr[n+1], s_len[n], s_split[n]   symmetric rows (lower ranks, then higher ranks)
+//   s_col[2m], s_eid[2m]               neighbour rank and edge id per symmetric entry
+//   o_ptr[n+1], o_col[m], e_src[m]     oriented CSR/COO; edge id = index
+//   sorted_entry[2m]                   input entry index of each symmetric entry
+
+#include "kt_device.cuh"
+#include "kt_engine.h"
+
+namespace kt {
+
+namespace {
+
+constexpr int kThreads = 256;
+
+inline uint32_t grid_for(uint64_t n, int threads = kThreads) {
+    uint64_t b = (n + threads - 1) / threads;
+    return (uint32_t)(b == 0 ? 1 : b);
+}
+
+__global__ void k_degree(const uint32_t* __restrict__ src, const uint32_t* __restrict__ dst, uint64_t entries,
+                         uint32_t n, uint32_t* __restrict__ deg, uint32_t* __restrict__ ctrl) {
+    uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t err = 0;
+    if (i < entries) {
+        uint32_t s = src[i], d = dst[i];
+        if (s >= n || d >= n) err = kErrBadVertex;
+        else {
+            if (s == d) err = kErrSelfLoop;
+            atomicAdd(&deg[s], 1u);
+        }
+    }
+    err = __reduce_or_sync(kFullMask, err);
+    if (err && lane_id() == 0) atomicOr(&ctrl[kCtrlError], err);
+}
+
+__global__ void k_rank_keys(const uint32_t* __restrict__ deg, uint32_t n, unsigned vb, uint64_t* __restrict__ keys) {
+    uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v < n) keys[v] = ((uint64_t)deg[v] << vb) | v;
+}
+
+// rank[v] = sorted position; row_len[rank] = degree (row lengths of the symmetric CSR).
+__global__ void k_rank_scatter(const uint64_t* __restrict__ sorted, uint32_t n, unsigned vb,
+                               uint32_t* __restrict__ rank, uint32_t* __restrict__ row_len) {
+    uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < n) {
+        uint64_t key = sorted[p];
+        rank[(uint32_t)(key & ((1ull << vb) - 1))] = p;
+        row_len[p] = (uint32_t)(key >> vb);
+    } else if (p == n) {
+        row_len[n] = 0;
+    }
+}
+
+__global__ void k_edge_keys(const uint32_t* __restrict__ src, const uint32_t* __restrict__ dst, uint64_t entries,
+                            const uint32_t* __restrict__ rank, unsigned vb, uint64_t* __restrict__ keys,
+                            uint32_t* __restrict__ vals) {
+    uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < entries) {
+        keys[i] = ((uint64_t)rank[src[i]] << vb) | rank[dst[i]];
+        vals[i] = (uint32_t)i;
+    }
+}
+
+__global__ void k_split_init(const uint32_t* __restrict__ s_ptr, uint32_t n, uint32_t* __restrict__ s_split,
+                             uint32_t* __restrict__ s_len) {
+    uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r < n) {
+        s_split[r] = s_ptr[r + 1];
+        s_len[r] = s_ptr[r + 1] - s_ptr[r];
+    }
+}
+
+// Neighbour column, duplicate check and the start of each row's higher-rank part.
+__global__ void k_csr_fill(const uint64_t* __restrict__ keys, uint64_t entries, unsigned vb,
+                           const uint32_t* __restrict__ s_ptr, uint32_t* __restrict__ s_col,
+                           uint32_t* __restrict__ s_split, uint32_t* __restrict__ ctrl) {
+    uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t err = 0;
+    if (p < entries) {
+        const uint64_t mask = (1ull << vb) - 1;
+        uint64_t key = keys[p];
+        uint32_t row = (uint32_t)(key >> vb), col = (uint32_t)(key & mask);
+        s_col[p] = col;
+        uint64_t prev = p > 0 ? keys[p - 1] : ~0ull;
+        if (p > 0 && prev == key) err = kErrDuplicate;
+        if (col > row && (p == s_ptr[row] || (uint32_t)(prev >> vb) != row || (uint32_t)(prev & mask) < row))
+            s_split[row] = (uint32_t)p;
+    }
+    err = __reduce_or_sync(kFullMask, err);
+    if (err && lane_id() == 0) atomicOr(&ctrl[kCtrlError], err);
+}
+
+__global__ void k_out_len(const uint32_t* __restrict__ s_ptr, const uint32_t* __restrict__ s_split, uint32_t n,
+                          uint32_t* __restrict__ out_len) {
+    uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r < n) out_len[r] = s_ptr[r + 1] - s_split[r];
+    else if (r == n) out_len[n] = 0;
+}
+
+// Higher-rank entries become oriented edges; their edge id is their oriented position.
+__global__ void k_orient(const uint64_t* __restrict__ keys, uint64_t entries, unsigned vb,
+                         const uint32_t* __restrict__ s_split, const uint32_t* __restrict__ o_ptr,
+                         uint32_t* __restrict__ o_col, uint32_t* __restrict__ e_src, uint32_t* __restrict__ s_eid,
+                         uint32_t m) {
+    uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < entries) {
+        uint64_t key = keys[p];
+        uint32_t row = (uint32_t)(key >> vb), col = (uint32_t)(key & ((1ull << vb) - 1));
+        if (col > row) {
+            uint32_t j = o_ptr[row] + (uint32_t)(p - s_split[row]);
+            if (j < m) {
+                o_col[j] = col;
+                e_src[j] = row;
+                s_eid[p] = j;
+            }
+        }
+    }
+}
+
+// Lower-rank entries (row r, column c < r) take the id of edge (c, r) from c's oriented row.
+__global__ void k_in_eid(const uint64_t* __restrict__ keys, uint64_t entries, unsigned vb,
+                         const uint32_t* __restrict__ o_ptr, const uint32_t* __restrict__ o_col,
+                         uint32_t* __restrict__ s_eid, uint32_t* __restrict__ ctrl) {
+    uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t err = 0;
+    if (p < entries) {
+        uint64_t key = keys[p];
+        uint32_t row = (uint32_t)(key >> vb), col = (uint32_t)(key & ((1ull << vb) - 1));
+        if (col < row) {
+            uint32_t lo = o_ptr[col], len = o_ptr[col + 1] - lo;
+            uint32_t idx = lower_bound_u32(o_col + lo, len, row);
+            if (idx < len && o_col[lo + idx] == row) s_eid[p] = lo + idx;
+            else { s_eid[p] = 0; err = kErrAsymmetric; }
+        }
+    }
+    err = __reduce_or_sync(kFullMask, err);
+    if (err && lane_id() == 0) atomicOr(&ctrl[kCtrlError], err);
+}
+
+unsigned bits_for(uint64_t n) {
+    unsigned b = 1;
+    while (b < 64 && (1ull << b) < n) ++b;
+    return b;
+}
+
+int error_status(uint32_t err) {
+    if (err & kErrBadVertex) return fail(KT_ERR_INVALID_ARG, "an entry names a vertex id >= num_nodes");
+    if (err & kErrSelfLoop) return fail(KT_ERR_SELF_LOOP, "Edges from a vertex to itself are not allowed!");
+    if (err & kErrDuplicate) return fail(KT_ERR_NOT_SYMMETRIC, "duplicate entry in the input edge list");
+    if (err & kErrAsymmetric) return fail(KT_ERR_NOT_SYMMETRIC, "entry (u,v) without its reverse (v,u)");
+    if (err & kErrTimeout) return fail(KT_ERR_TIMEOUT, "a bounded device wait expired");
+    return KT_OK;
+}
+
+// Synchronizes and converts the device error word into a status.
+int sync_and_check(kt_engine* e) {
+    int rc = check_cuda(cudaMemcpyAsync(e->h_ctrl, e->ctrl, sizeof(uint32_t) * kCtrlWords, cudaMemcpyDeviceToHost,
+                                        e->stream), "read control block");
+    if (rc) return rc;
+    rc = check_cuda(cudaStreamSynchronize(e->stream), "build synchronize");
+    if (rc) return rc;
+    return error_status(e->h_ctrl[kCtrlError]);
+}
+
+}  // namespace
+
+int build_graph(kt_engine* e, const uint32_t* d_src, const uint32_t* d_dst, uint64_t entries, uint32_t n) {
+    if (entries & 1) return fail(KT_ERR_NOT_SYMMETRIC, "odd number of entries (%llu): every edge needs both directions",
+                                 (unsigned long long)entries);
+    if (entries >= 0xffffffffull) return fail(KT_ERR_TOO_LARGE, "more than 2^32-2 entries");
+    if (n > e->cap_nodes || entries > e->cap_entries) {
+        int rc = reserve(e, n > e->cap_nodes ? n : e->cap_nodes, entries > e->cap_entries ? entries : e->cap_entries);
+        if (rc) return rc;
+    }
+    e->n = n;
+    e->entries = entries;
+    e->m = (uint32_t)(entries / 2);
+    e->vb = bits_for(n > 1 ? n : 2);
+    const unsigned vb = e->vb;
+    cudaStream_t st = e->stream;
+    int rc = check_cuda(cudaMemsetAsync(e->ctrl, 0, sizeof(uint32_t) * kCtrlWords, st), "clear control block");
+    if (rc) return rc;
+    if (n == 0) return entries ? fail(KT_ERR_INVALID_ARG, "entries given for a graph with 0 vertices") : KT_OK;
+
+    // 1. degrees (and id / self-loop checks)
+    rc = check_cuda(cudaMemsetAsync(e->deg, 0, sizeof(uint32_t) * n, st), "clear degrees");
+    if (rc) return rc;
+    if (entries) {
+        k_degree<<<grid_for(entries), kThreads, 0, st>>>(d_src, d_dst, entries, n, e->deg, e->ctrl);
+        count_launch(e);
+        if ((rc = check_launch(e, "k_degree"))) return rc;
+    }
+    if ((rc = sync_and_check(e))) return rc;
+
+    // 2. ranks: ascending (degree, id)
+    k_rank_keys<<<grid_for(n), kThreads, 0, st>>>(e->deg, n, vb, e->key_a);
+    count_launch(e);
+    if ((rc = check_launch(e, "k_rank_keys"))) return rc;
+    int in_b = 0;
+    if ((rc = radix_sort(e, e->key_a, nullptr, e->key_b, nullptr, n, vb + bits_for(entries + 2), &in_b))) return rc;
+    k_rank_scatter<<<grid_for((uint64_t)n + 1), kThreads, 0, st>>>(in_b ? e->key_b : e->key_a, n, vb, e->rank,
+                                                                   e->s_len);
+    count_launch(e);
+    if ((rc = check_launch(e, "k_rank_scatter"))) return rc;
+    // row starts of the symmetric CSR (row r holds the neighbours of the rank-r vertex)
+    if ((rc = exclusive_scan(e, e->s_len, e->s_ptr, (uint64_t)n + 1))) return rc;
+
+    // 3. sort entries by (rank[src], rank[dst])
+    if (entries) {
+        k_edge_keys<<<grid_for(entries), kThreads, 0, st>>>(d_src, d_dst, entries, e->rank, vb, e->key_a, e->val_a);
+        count_launch(e);
+        if ((rc = check_launch(e, "k_edge_keys"))) return rc;
+        if ((rc = radix_sort(e, e->key_a, e->val_a, e->key_b, e->val_b, entries, 2 * vb, &in_b))) return rc;
+    }
+    const uint64_t* keys = in_b ? e->key_b : e->key_a;
+    e->sorted_entry = in_b ? e->val_b : e->val_a;
+
+    // 4. columns, split points, oriented CSR, edge ids
+    k_split_init<<<grid_for(n), kThreads, 0, st>>>(e->s_ptr, n, e->s_split, e->s_len);
+    count_launch(e);
+    if ((rc = check_launch(e, "k_split_init"))) return rc;
+    if (entries) {
+        k_csr_fill<<<grid_for(entries), kThreads, 0, st>>>(keys, entries, vb, e->s_ptr, e->s_col, e->s_split, e->ctrl);
+        count_launch(e);
+        if ((rc = check_launch(e, "k_csr_fill"))) return rc;
+    }
+    k_out_len<<<grid_for((uint64_t)n + 1), kThreads, 0, st>>>(e->s_ptr, e->s_split, n, e->o_ptr);
+    count_launch(e);
+    if ((rc = check_launch(e, "k_out_len"))) return rc;
+    if ((rc = exclusive_scan(e, e->o_ptr, e->o_ptr, (uint64_t)n + 1))) return rc;
+    if (entries) {
+        k_orient<<<grid_for(entries), kThreads, 0, st>>>(keys, entries, vb, e->s_split, e->o_ptr, e->o_col, e->e_src,
+                                                         e->s_eid, e->m);
+        count_launch(e);
+        if ((rc = check_launch(e, "k_orient"))) return rc;
+    }
+    // the oriented CSR must hold exactly half the entries before its rows are searched
+    uint32_t m_out = 0;
+    if ((rc = check_cuda(cudaMemcpyAsync(&m_out, e->o_ptr + n, sizeof(uint32_t), cudaMemcpyDeviceToHost, st),
+                         "read edge count")))
+        return rc;
+    if ((rc = sync_and_check(e))) return rc;
+    if (m_out != e->m)
+        return fail(KT_ERR_NOT_SYMMETRIC, "%u entries point to higher-degree-rank vertices, %u to lower ones", m_out,
+                    (uint32_t)(entries - m_out));
+    if (entries) {
+        k_in_eid<<<grid_for(entries), kThreads, 0, st>>>(keys, entries, vb, e->o_ptr, e->o_col, e->s_eid, e->ctrl);
+        count_launch(e);
+        if ((rc = check_launch(e, "k_in_eid"))) return rc;
+    }
+    return sync_and_check(e);
+}
+
+}  // namespace kt

@@ -1,0 +1,372 @@
+// Engine lifecycle, workspace layout and the C ABI of the k-truss path.
+//
+// kt_ktruss / kt_decompose take host buffers like the reference's ktruss() (kernel.h:12):
+// they copy the graph to the device, run the device pipeline and copy the result back.
+// kt_engine_* take device buffers and leave the data in HBM.
+
+#include <algorithm>
+#include <chrono>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "kt_device.cuh"
+#include "kt_engine.h"
+
+namespace kt {
+
+int check_cuda(cudaError_t err, const char* what) {
+    if (err == cudaSuccess) return KT_OK;
+    int code = (err == cudaErrorMemoryAllocation) ? KT_ERR_DEVICE_ALLOC
+               : (err == cudaErrorNoDevice || err == cudaErrorInsufficientDriver) ? KT_ERR_NO_DEVICE
+                                                                                 : KT_ERR_CUDA;
+    return fail(code, "%s: %s", what, cudaGetErrorString(err));
+}
+
+int check_launch(kt_engine*, const char* what) { return check_cuda(cudaGetLastError(), what); }
+
+namespace {
+
+size_t align_up(size_t x) { return (x + 255) & ~(size_t)255; }
+
+struct Carver {
+    char* base;
+    size_t off = 0;
+    template <class T>
+    T* take(size_t count) {
+        T* p = reinterpret_cast<T*>(base ? base + off : nullptr);
+        off += align_up(sizeof(T) * (count ? count : 1));
+        return p;
+    }
+};
+
+// Lays out every array of the engine for the given capacity; with base == nullptr it only
+// measures the arena.
+size_t carve(kt_engine* e, char* base, uint32_t n, uint64_t N) {
+    const uint64_t m = N / 2 + 1;
+    const uint64_t keys = std::max<uint64_t>(N, n);
+    const uint64_t sort_blocks = (keys + 2047) / 2048;
+    const uint64_t hist_words = 256 * sort_blocks;
+    const uint64_t scan_max = std::max<uint64_t>((uint64_t)n + 1, hist_words);
+    const uint64_t scan_words = scan_max / 4096 + 4096;
+    Carver c{base};
+    e->key_a = c.take<uint64_t>(keys);
+    e->key_b = c.take<uint64_t>(keys);
+    e->val_a = c.take<uint32_t>(N);
+    e->val_b = c.take<uint32_t>(N);
+    e->deg = c.take<uint32_t>(n);
+    e->rank = c.take<uint32_t>(n);
+    e->s_ptr = c.take<uint32_t>((size_t)n + 1);
+    e->s_len = c.take<uint32_t>((size_t)n + 1);
+    e->s_split = c.take<uint32_t>((size_t)n + 1);
+    e->o_ptr = c.take<uint32_t>((size_t)n + 1);
+    e->s_col = c.take<uint32_t>(N);
+    e->s_eid = c.take<uint32_t>(N);
+    e->o_col = c.take<uint32_t>(m);
+    e->e_src = c.take<uint32_t>(m);
+    e->sup = c.take<uint32_t>(m);
+    e->rnd = c.take<uint32_t>(m);
+    e->tr = c.take<uint32_t>(m);
+    e->q0 = c.take<uint32_t>(m);
+    e->q1 = c.take<uint32_t>(m);
+    e->alive0 = c.take<uint32_t>(m);
+    e->alive1 = c.take<uint32_t>(m);
+    e->hist = c.take<uint32_t>(hist_words);
+    e->hist_words = hist_words;
+    e->scan_tmp = c.take<uint32_t>(scan_words);
+    e->scan_tmp_words = scan_words;
+    e->in_src = c.take<uint32_t>(N);
+    e->in_dst = c.take<uint32_t>(N);
+    e->out_u32 = c.take<uint32_t>(N);
+    e->out_u8 = c.take<uint8_t>(N);
+    return c.off;
+}
+
+}  // namespace
+
+int reserve(kt_engine* e, uint32_t max_nodes, uint64_t max_entries) {
+    if (max_nodes <= e->cap_nodes && max_entries <= e->cap_entries && e->arena) return KT_OK;
+    max_nodes = std::max(max_nodes, e->cap_nodes);
+    max_entries = std::max(max_entries, e->cap_entries);
+    int rc = check_cuda(cudaSetDevice(e->device), "cudaSetDevice");
+    if (rc) return rc;
+    if (e->arena) {
+        if ((rc = check_cuda(cudaStreamSynchronize(e->stream), "synchronize before resize"))) return rc;
+        cudaFree(e->arena);
+        e->arena = nullptr;
+        e->arena_bytes = 0;
+    }
+    const size_t bytes = carve(e, nullptr, max_nodes, max_entries);
+    void* p = nullptr;
+    if ((rc = check_cuda(cudaMalloc(&p, bytes), "allocate engine workspace"))) {
+        e->cap_nodes = 0;
+        e->cap_entries = 0;
+        return rc;
+    }
+    e->arena = p;
+    e->arena_bytes = bytes;
+    carve(e, static_cast<char*>(p), max_nodes, max_entries);
+    e->cap_nodes = max_nodes;
+    e->cap_entries = max_entries;
+    return KT_OK;
+}
+
+}  // namespace kt
+
+using kt::check_cuda;
+using kt::fail;
+
+namespace {
+
+std::mutex g_default_mu;
+kt_engine* g_default = nullptr;
+
+// The engine used by the host-buffer entry points (device 0, created on first use).
+int default_engine(kt_engine** out) {
+    std::lock_guard<std::mutex> lock(g_default_mu);
+    if (!g_default) {
+        int rc = kt_engine_create(0, &g_default);
+        if (rc) return rc;
+    }
+    *out = g_default;
+    return KT_OK;
+}
+
+double now_ms() {
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+int record_start(kt_engine* e) { return check_cuda(cudaEventRecord(e->ev_start, e->stream), "record start"); }
+
+int record(kt_engine* e, cudaEvent_t ev) { return check_cuda(cudaEventRecord(ev, e->stream), "record event"); }
+
+int record_stop(kt_engine* e) {
+    int rc = check_cuda(cudaEventRecord(e->ev_stop, e->stream), "record stop");
+    if (rc) return rc;
+    if ((rc = check_cuda(cudaEventSynchronize(e->ev_stop), "synchronize stop"))) return rc;
+    float a = 0, b = 0, c = 0;
+    if ((rc = check_cuda(cudaEventElapsedTime(&a, e->ev_start, e->ev_built), "elapsed time")) ||
+        (rc = check_cuda(cudaEventElapsedTime(&b, e->ev_built, e->ev_counted), "elapsed time")) ||
+        (rc = check_cuda(cudaEventElapsedTime(&c, e->ev_counted, e->ev_stop), "elapsed time")))
+        return rc;
+    e->stats.build_ms = a;
+    e->stats.support_ms = b;
+    e->stats.peel_ms = c;
+    e->stats.last_ms = a + b + c;
+    return KT_OK;
+}
+
+int fill_graph_stats(kt_engine* e) {
+    e->stats.num_nodes = e->n;
+    e->stats.num_edges = e->m;
+    e->stats.kernel_launches = e->launches;
+    return KT_OK;
+}
+
+// Device pipeline for the decomposition (inputs on the device).
+int run_decompose(kt_engine* e, const uint32_t* d_src, const uint32_t* d_dst, uint64_t entries, uint32_t n,
+                  uint32_t* d_truss, uint32_t* d_k_max) {
+    int rc;
+    if ((rc = record_start(e))) return rc;
+    if ((rc = kt::build_graph(e, d_src, d_dst, entries, n))) return rc;
+    if ((rc = record(e, e->ev_built))) return rc;
+    if ((rc = kt::count_support(e))) return rc;
+    if ((rc = record(e, e->ev_counted))) return rc;
+    if ((rc = kt::peel_decompose(e))) return rc;
+    if ((rc = kt::emit_truss_per_entry(e, d_truss, d_k_max))) return rc;
+    if ((rc = record_stop(e))) return rc;
+    return fill_graph_stats(e);
+}
+
+int run_ktruss(kt_engine* e, const uint32_t* d_src, const uint32_t* d_dst, uint64_t entries, uint32_t n, uint32_t k,
+               uint8_t* d_keep) {
+    int rc;
+    if ((rc = record_start(e))) return rc;
+    if ((rc = kt::build_graph(e, d_src, d_dst, entries, n))) return rc;
+    if ((rc = record(e, e->ev_built))) return rc;
+    if (k >= 3) {
+        if ((rc = kt::count_support(e))) return rc;
+    }
+    if ((rc = record(e, e->ev_counted))) return rc;
+    if ((rc = kt::peel_single_k(e, k))) return rc;
+    if ((rc = kt::emit_keep(e, d_keep))) return rc;
+    if ((rc = record_stop(e))) return rc;
+    return fill_graph_stats(e);
+}
+
+int check_coo(const kt_coo* g, const char* what) {
+    if (!g) return fail(KT_ERR_INVALID_ARG, "%s: null graph", what);
+    if (g->num_edges && (!g->src_idx || !g->dst_idx)) return fail(KT_ERR_INVALID_ARG, "%s: null edge arrays", what);
+    return KT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int kt_engine_create(int device, kt_engine** out) {
+    if (!out) return fail(KT_ERR_INVALID_ARG, "kt_engine_create: null output");
+    *out = nullptr;
+    int count = 0;
+    int rc = check_cuda(cudaGetDeviceCount(&count), "cudaGetDeviceCount");
+    if (rc) return rc;
+    if (device < 0 || device >= count) return fail(KT_ERR_NO_DEVICE, "device %d not present (%d devices)", device, count);
+    if ((rc = check_cuda(cudaSetDevice(device), "cudaSetDevice"))) return rc;
+    kt_engine* e = new kt_engine();
+    e->device = device;
+    if ((rc = check_cuda(cudaDeviceGetAttribute(&e->num_sms, cudaDevAttrMultiProcessorCount, device), "SM count")) ||
+        (rc = check_cuda(cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking), "create stream")) ||
+        (rc = check_cuda(cudaEventCreate(&e->ev_start), "create event")) ||
+        (rc = check_cuda(cudaEventCreate(&e->ev_stop), "create event")) ||
+        (rc = check_cuda(cudaEventCreate(&e->ev_built), "create event")) ||
+        (rc = check_cuda(cudaEventCreate(&e->ev_counted), "create event")) ||
+        (rc = check_cuda(cudaMalloc(&e->ctrl, sizeof(uint32_t) * kt::kCtrlWords), "allocate control block")) ||
+        (rc = check_cuda(cudaMallocHost(&e->h_ctrl, sizeof(uint32_t) * kt::kCtrlWords), "allocate host mirror"))) {
+        kt_engine_destroy(e);
+        return rc;
+    }
+    *out = e;
+    return KT_OK;
+}
+
+int kt_engine_destroy(kt_engine* e) {
+    if (!e) return KT_OK;
+    cudaSetDevice(e->device);
+    if (e->stream) cudaStreamSynchronize(e->stream);
+    if (e->arena) cudaFree(e->arena);
+    if (e->ctrl) cudaFree(e->ctrl);
+    if (e->h_ctrl) cudaFreeHost(e->h_ctrl);
+    if (e->ev_start) cudaEventDestroy(e->ev_start);
+    if (e->ev_stop) cudaEventDestroy(e->ev_stop);
+    if (e->ev_built) cudaEventDestroy(e->ev_built);
+    if (e->ev_counted) cudaEventDestroy(e->ev_counted);
+    if (e->stream) cudaStreamDestroy(e->stream);
+    delete e;
+    return KT_OK;
+}
+
+void* kt_engine_stream(kt_engine* e) { return e ? (void*)e->stream : nullptr; }
+
+int kt_engine_reserve(kt_engine* e, uint32_t max_nodes, uint64_t max_entries) {
+    if (!e) return fail(KT_ERR_INVALID_ARG, "kt_engine_reserve: null engine");
+    if (max_entries >= 0xffffffffull) return fail(KT_ERR_TOO_LARGE, "more than 2^32-2 entries");
+    return kt::reserve(e, max_nodes, max_entries);
+}
+
+int kt_engine_decompose(kt_engine* e, const uint32_t* d_src, const uint32_t* d_dst, uint64_t num_entries,
+                        uint32_t num_nodes, uint32_t* d_truss, uint32_t* d_k_max, int sync) {
+    if (!e) return fail(KT_ERR_INVALID_ARG, "kt_engine_decompose: null engine");
+    if (num_entries && (!d_src || !d_dst || !d_truss)) return fail(KT_ERR_INVALID_ARG, "kt_engine_decompose: null buffer");
+    kt::clear_error();
+    int rc = check_cuda(cudaSetDevice(e->device), "cudaSetDevice");
+    if (rc) return rc;
+    if ((rc = run_decompose(e, d_src, d_dst, num_entries, num_nodes, d_truss, d_k_max))) return rc;
+    if (sync) return check_cuda(cudaStreamSynchronize(e->stream), "synchronize");
+    return KT_OK;
+}
+
+int kt_engine_ktruss(kt_engine* e, const uint32_t* d_src, const uint32_t* d_dst, uint64_t num_entries,
+                     uint32_t num_nodes, uint32_t k, uint8_t* d_keep, int sync) {
+    if (!e) return fail(KT_ERR_INVALID_ARG, "kt_engine_ktruss: null engine");
+    if (num_entries && (!d_src || !d_dst || !d_keep)) return fail(KT_ERR_INVALID_ARG, "kt_engine_ktruss: null buffer");
+    kt::clear_error();
+    int rc = check_cuda(cudaSetDevice(e->device), "cudaSetDevice");
+    if (rc) return rc;
+    if ((rc = run_ktruss(e, d_src, d_dst, num_entries, num_nodes, k, d_keep))) return rc;
+    if (sync) return check_cuda(cudaStreamSynchronize(e->stream), "synchronize");
+    return KT_OK;
+}
+
+int kt_engine_stats(kt_engine* e, kt_stats* stats) {
+    if (!e || !stats) return fail(KT_ERR_INVALID_ARG, "kt_engine_stats: null argument");
+    int rc = check_cuda(cudaStreamSynchronize(e->stream), "synchronize");
+    if (rc) return rc;
+    e->stats.kernel_launches = e->launches;
+    *stats = e->stats;
+    return KT_OK;
+}
+
+int kt_decompose(const kt_coo* graph, uint32_t* truss_per_entry, uint32_t* k_max, const kt_config* config) {
+    int rc = check_coo(graph, "kt_decompose");
+    if (rc) return rc;
+    if (graph->num_edges && !truss_per_entry) return fail(KT_ERR_INVALID_ARG, "kt_decompose: null output");
+    if (config && config->processor == KT_PROCESSOR_CPU)
+        return fail(KT_ERR_UNSUPPORTED, "processor cpu: this library runs the GPU path only");
+    kt::clear_error();
+    kt_engine* e = nullptr;
+    if ((rc = default_engine(&e))) return rc;
+    std::lock_guard<std::mutex> lock(g_default_mu);
+    if ((rc = check_cuda(cudaSetDevice(e->device), "cudaSetDevice"))) return rc;
+    const uint64_t N = graph->num_edges;
+    if ((rc = kt::reserve(e, std::max(graph->num_nodes, e->cap_nodes), std::max(N, e->cap_entries)))) return rc;
+    if (N) {
+        if ((rc = check_cuda(cudaMemcpyAsync(e->in_src, graph->src_idx, N * 4, cudaMemcpyHostToDevice, e->stream), "H2D")) ||
+            (rc = check_cuda(cudaMemcpyAsync(e->in_dst, graph->dst_idx, N * 4, cudaMemcpyHostToDevice, e->stream), "H2D")))
+            return rc;
+    }
+    if ((rc = run_decompose(e, e->in_src, e->in_dst, N, graph->num_nodes, e->out_u32, nullptr))) return rc;
+    if (N && (rc = check_cuda(cudaMemcpyAsync(truss_per_entry, e->out_u32, N * 4, cudaMemcpyDeviceToHost, e->stream), "D2H")))
+        return rc;
+    if ((rc = check_cuda(cudaStreamSynchronize(e->stream), "synchronize"))) return rc;
+    if (k_max) *k_max = e->stats.k_max;
+    return KT_OK;
+}
+
+int kt_ktruss(const kt_coo* graph, kt_coo* truss, const kt_config* config) {
+    int rc = check_coo(graph, "kt_ktruss");
+    if (rc) return rc;
+    if (!truss || !config) return fail(KT_ERR_INVALID_ARG, "kt_ktruss: null truss or config");
+    if (config->processor == KT_PROCESSOR_CPU)
+        return fail(KT_ERR_UNSUPPORTED, "processor cpu: this library runs the GPU path only");
+    if (config->processor != KT_PROCESSOR_GPU || config->directedness < 0 || config->directedness > 2 ||
+        config->input_format < 0 || config->input_format > 1 || config->recount < 0 || config->recount > 1)
+        return fail(KT_ERR_INVALID_ARG, "kt_ktruss: bad enum value in config");
+    if (truss->capacity < graph->num_edges || (graph->num_edges && (!truss->src_idx || !truss->dst_idx)))
+        return fail(KT_ERR_CAPACITY, "truss capacity %u below %u entries", truss->capacity, graph->num_edges);
+    kt::clear_error();
+    kt_engine* e = nullptr;
+    if ((rc = default_engine(&e))) return rc;
+    std::lock_guard<std::mutex> lock(g_default_mu);
+    if ((rc = check_cuda(cudaSetDevice(e->device), "cudaSetDevice"))) return rc;
+    const uint64_t N = graph->num_edges;
+    const int verbose = config->verbosity >= 1;
+    double t0 = now_ms();
+    if ((rc = kt::reserve(e, std::max(graph->num_nodes, e->cap_nodes), std::max(N, e->cap_entries)))) return rc;
+    if (N) {
+        if ((rc = check_cuda(cudaMemcpyAsync(e->in_src, graph->src_idx, N * 4, cudaMemcpyHostToDevice, e->stream), "H2D")) ||
+            (rc = check_cuda(cudaMemcpyAsync(e->in_dst, graph->dst_idx, N * 4, cudaMemcpyHostToDevice, e->stream), "H2D")) ||
+            (rc = check_cuda(cudaStreamSynchronize(e->stream), "synchronize")))
+            return rc;
+    }
+    if (verbose) printf("    Copy COO graph to GPU: %f ms\n", now_ms() - t0);
+    // -w warm-up and -x timed runs (kernel_ddc.cu:227-244); each run rebuilds the graph from
+    // the input entries, so every run is the full device pipeline.
+    const uint32_t runs = config->num_warmup_runs + config->num_timed_runs;
+    for (uint32_t i = 0; i < (runs ? runs : 1); ++i) {
+        if (verbose) printf("    Performing K-truss\n");
+        if ((rc = run_ktruss(e, e->in_src, e->in_dst, N, graph->num_nodes, config->k, e->out_u8))) return rc;
+        if (config->verbosity == 0 && i >= config->num_warmup_runs) {
+            kt_print_config_csv(config);
+            printf("%f ms\n", e->stats.last_ms);
+        }
+        if (verbose) printf("\033[0;32m        Total K-truss time: %f ms\n\033[0m", e->stats.last_ms);
+    }
+    t0 = now_ms();
+    std::vector<uint8_t> keep(N);
+    if (N && (rc = check_cuda(cudaMemcpyAsync(keep.data(), e->out_u8, N, cudaMemcpyDeviceToHost, e->stream), "D2H")))
+        return rc;
+    if ((rc = check_cuda(cudaStreamSynchronize(e->stream), "synchronize"))) return rc;
+    uint32_t w = 0;
+    for (uint64_t i = 0; i < N; ++i)
+        if (keep[i]) {
+            truss->src_idx[w] = graph->src_idx[i];
+            truss->dst_idx[w] = graph->dst_idx[i];
+            ++w;
+        }
+    truss->num_edges = w;
+    truss->num_nodes = graph->num_nodes;
+    if (verbose) printf("    Copy COO truss from GPU: %f ms\n", now_ms() - t0);
+    return KT_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,105 @@
+// The device-resident engine: workspace layout in HBM and the internal stages.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <vector>
+
+#include "kt_internal.h"
+
+struct kt_engine {
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev_start = nullptr, ev_stop = nullptr, ev_built = nullptr, ev_counted = nullptr;
+    uint64_t launches = 0;
+
+    // Workspace arena: one allocation carved into the arrays below.
+    void* arena = nullptr;
+    size_t arena_bytes = 0;
+    uint32_t cap_nodes = 0;
+    uint64_t cap_entries = 0;
+
+    // Sort buffers (2m entries): keys (src_rank << vb | dst_rank) and entry indices.
+    uint64_t* key_a = nullptr;
+    uint64_t* key_b = nullptr;
+    uint32_t* val_a = nullptr;
+    uint32_t* val_b = nullptr;
+    // Per vertex (rank space unless noted).
+    uint32_t* deg = nullptr;      // degree by original id
+    uint32_t* rank = nullptr;     // original id -> rank
+    uint32_t* s_ptr = nullptr;    // n+1: symmetric CSR row starts
+    uint32_t* s_len = nullptr;    // n: live length of each symmetric row (after compaction)
+    uint32_t* s_split = nullptr;  // n: first position of the row's higher-rank neighbours
+    uint32_t* o_ptr = nullptr;    // n+1: oriented CSR row starts (edge id of a row's first edge)
+    // Per symmetric entry (2m).
+    uint32_t* s_col = nullptr;    // neighbour rank
+    uint32_t* s_eid = nullptr;    // edge id of the entry
+    uint32_t* sorted_entry = nullptr;  // input entry index at this sorted position
+    // Per edge (m); edge id = position in the oriented CSR.
+    uint32_t* o_col = nullptr;    // higher-rank endpoint
+    uint32_t* e_src = nullptr;    // lower-rank endpoint
+    uint32_t* sup = nullptr;      // support (alive triangles)
+    uint32_t* rnd = nullptr;      // 0 while alive, else the peel round that removed it
+    uint32_t* tr = nullptr;       // truss number (written at removal)
+    uint32_t* q0 = nullptr;       // frontier queues
+    uint32_t* q1 = nullptr;
+    uint32_t* alive0 = nullptr;   // compacted lists of alive edge ids
+    uint32_t* alive1 = nullptr;
+    // Scratch for scans and sort histograms.
+    uint32_t* scan_tmp = nullptr;
+    size_t scan_tmp_words = 0;
+    uint32_t* hist = nullptr;
+    size_t hist_words = 0;
+    // Control block (device) and its pinned host mirror.
+    uint32_t* ctrl = nullptr;
+    uint32_t* h_ctrl = nullptr;
+    // Per-round log: frontier size and level of each peel round.
+    uint32_t* round_size = nullptr;
+    uint32_t* round_level = nullptr;
+    uint32_t cap_rounds = 0;
+    // Staging for the host-buffer entry points.
+    uint32_t* in_src = nullptr;
+    uint32_t* in_dst = nullptr;
+    uint32_t* out_u32 = nullptr;
+    uint8_t* out_u8 = nullptr;
+
+    // Current graph.
+    uint32_t n = 0;
+    uint64_t entries = 0;
+    uint32_t m = 0;
+    uint32_t vb = 1;  // bits per rank in sort keys
+
+    kt_stats stats{};
+};
+
+namespace kt {
+
+// Launch bookkeeping: every kernel launch of the engine goes through this.
+inline void count_launch(kt_engine* e, uint64_t n = 1) { e->launches += n; }
+int check_cuda(cudaError_t err, const char* what);
+int check_launch(kt_engine* e, const char* what);
+
+int reserve(kt_engine* e, uint32_t max_nodes, uint64_t max_entries);
+
+// kt_sort.cu
+int exclusive_scan(kt_engine* e, const uint32_t* in, uint32_t* out, uint64_t n);
+// Sorts (keys, vals) by the low `bits` bits of the keys; ping-pongs between a and b buffers
+// and returns 0 if the result is in (key_a, val_a), 1 if in (key_b, val_b).  vals may be null.
+int radix_sort(kt_engine* e, uint64_t* key_a, uint32_t* val_a, uint64_t* key_b, uint32_t* val_b,
+               uint64_t n, unsigned bits, int* result_in_b);
+
+// kt_build.cu: relabel by degree, orient, sort, symmetric + oriented CSR, edge ids.
+int build_graph(kt_engine* e, const uint32_t* d_src, const uint32_t* d_dst, uint64_t entries, uint32_t n);
+
+// kt_support.cu: support of every edge (triangles through it) into e->sup.
+int count_support(kt_engine* e);
+
+// kt_peel.cu
+int peel_decompose(kt_engine* e);
+int peel_single_k(kt_engine* e, uint32_t k);
+int emit_truss_per_entry(kt_engine* e, uint32_t* d_out, uint32_t* d_k_max);
+int emit_keep(kt_engine* e, uint8_t* d_keep);
+
+}  // namespace kt

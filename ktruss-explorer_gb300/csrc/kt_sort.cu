@@ -1,0 +1,228 @@
+// Device primitives for the CSR build: exclusive scan and a stable LSD radix sort.
+//
+// These replace the Thrust scan and the per-row CPU quicksort of the reference build
+// (graph.cu:457 thrust::exclusive_scan, graph.cu:462-476 "Sort outgoing edges ... on CPU").
+
+#include "kt_device.cuh"
+#include "kt_engine.h"
+
+namespace kt {
+
+namespace {
+
+constexpr int kScanThreads = 1024;
+constexpr int kScanItems = 4;
+constexpr uint32_t kScanTile = kScanThreads * kScanItems;  // 4096
+
+// Block-wide exclusive scan of one value per thread; returns the block total in *total.
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* warp_sums, uint32_t* total) {
+    const uint32_t lane = lane_id(), warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    uint32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(kFullMask, x, o);
+        if (lane >= (uint32_t)o) x += y;
+    }
+    if (lane == 31) warp_sums[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = lane < nwarps ? warp_sums[lane] : 0;
+        uint32_t s = w;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t y = __shfl_up_sync(kFullMask, s, o);
+            if (lane >= (uint32_t)o) s += y;
+        }
+        if (lane < nwarps) warp_sums[lane] = s - w;
+        if (lane == 31) warp_sums[32] = s;
+    }
+    __syncthreads();
+    uint32_t r = warp_sums[warp] + x - v;
+    *total = warp_sums[32];
+    __syncthreads();
+    return r;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_tile_sums(const uint32_t* __restrict__ in, uint64_t n,
+                                                                   uint32_t* __restrict__ sums) {
+    __shared__ uint32_t ws[33];
+    const uint64_t base = (uint64_t)blockIdx.x * kScanTile;
+    uint32_t s = 0;
+#pragma unroll
+    for (int i = 0; i < kScanItems; ++i) {
+        uint64_t idx = base + threadIdx.x + (uint64_t)i * kScanThreads;
+        if (idx < n) s += in[idx];
+    }
+    uint32_t total;
+    block_exclusive_scan(s, ws, &total);
+    if (threadIdx.x == 0) sums[blockIdx.x] = total;
+}
+
+// Exclusive scan of each tile, offset by the scanned tile sums (if given).
+__global__ void __launch_bounds__(kScanThreads) k_scan_tiles(const uint32_t* in, uint32_t* out, uint64_t n,
+                                                               const uint32_t* __restrict__ tile_offsets) {
+    __shared__ uint32_t tile[kScanTile];
+    __shared__ uint32_t ws[33];
+    const uint64_t base = (uint64_t)blockIdx.x * kScanTile;
+#pragma unroll
+    for (int i = 0; i < kScanItems; ++i) {
+        uint64_t idx = base + threadIdx.x + (uint64_t)i * kScanThreads;
+        tile[threadIdx.x + i * kScanThreads] = idx < n ? in[idx] : 0u;
+    }
+    __syncthreads();
+    uint32_t v[kScanItems], s = 0;
+#pragma unroll
+    for (int i = 0; i < kScanItems; ++i) {
+        v[i] = tile[threadIdx.x * kScanItems + i];
+        s += v[i];
+    }
+    uint32_t total;
+    uint32_t run = block_exclusive_scan(s, ws, &total) + (tile_offsets ? tile_offsets[blockIdx.x] : 0u);
+#pragma unroll
+    for (int i = 0; i < kScanItems; ++i) {
+        tile[threadIdx.x * kScanItems + i] = run;
+        run += v[i];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < kScanItems; ++i) {
+        uint64_t idx = base + threadIdx.x + (uint64_t)i * kScanThreads;
+        if (idx < n) out[idx] = tile[threadIdx.x + i * kScanThreads];
+    }
+}
+
+constexpr int kSortThreads = 256;
+constexpr int kSortWarps = kSortThreads / 32;
+constexpr int kSortSteps = 8;                           // 32-key steps per warp
+constexpr uint32_t kSortWarpKeys = 32 * kSortSteps;     // 256 keys per warp
+constexpr uint32_t kSortTile = kSortWarps * kSortWarpKeys;  // 2048 keys per block
+
+__global__ void __launch_bounds__(kSortThreads) k_radix_hist(const uint64_t* __restrict__ keys, uint64_t n,
+                                                               unsigned shift, uint32_t* __restrict__ hist,
+                                                               uint32_t num_blocks) {
+    __shared__ uint32_t h[256];
+    h[threadIdx.x] = 0;
+    __syncthreads();
+    const uint64_t base = (uint64_t)blockIdx.x * kSortTile;
+    for (uint32_t i = threadIdx.x; i < kSortTile; i += kSortThreads) {
+        uint64_t idx = base + i;
+        if (idx < n) atomicAdd(&h[(uint32_t)(keys[idx] >> shift) & 255u], 1u);
+    }
+    __syncthreads();
+    hist[(uint64_t)threadIdx.x * num_blocks + blockIdx.x] = h[threadIdx.x];
+}
+
+// Stable scatter of one 2048-key tile: each warp ranks its 256 consecutive keys in eight
+// 32-key steps with __match_any_sync; warps are then offset by the counts of earlier warps.
+__global__ void __launch_bounds__(kSortThreads) k_radix_scatter(const uint64_t* __restrict__ kin,
+                                                                  const uint32_t* __restrict__ vin,
+                                                                  uint64_t* __restrict__ kout,
+                                                                  uint32_t* __restrict__ vout, uint64_t n,
+                                                                  unsigned shift,
+                                                                  const uint32_t* __restrict__ hist,
+                                                                  uint32_t num_blocks) {
+    __shared__ uint32_t wh[kSortWarps][256];
+    __shared__ uint32_t goff[256];
+    const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
+    for (uint32_t i = threadIdx.x; i < kSortWarps * 256; i += kSortThreads) (&wh[0][0])[i] = 0;
+    goff[threadIdx.x] = hist[(uint64_t)threadIdx.x * num_blocks + blockIdx.x];
+    __syncthreads();
+    const uint64_t wbase = (uint64_t)blockIdx.x * kSortTile + (uint64_t)warp * kSortWarpKeys;
+    uint64_t key[kSortSteps];
+    uint32_t val[kSortSteps], dig[kSortSteps], rk[kSortSteps];
+#pragma unroll
+    for (int s = 0; s < kSortSteps; ++s) {
+        uint64_t idx = wbase + (uint32_t)s * 32 + lane;
+        bool valid = idx < n;
+        key[s] = valid ? kin[idx] : 0ull;
+        val[s] = (valid && vin) ? vin[idx] : 0u;
+        uint32_t d = valid ? ((uint32_t)(key[s] >> shift) & 255u) : 256u;
+        dig[s] = d;
+        uint32_t peers = __match_any_sync(kFullMask, d);
+        uint32_t base = d < 256 ? wh[warp][d] : 0u;
+        __syncwarp();
+        if (d < 256 && lane == (uint32_t)(__ffs(peers) - 1)) wh[warp][d] = base + __popc(peers);
+        __syncwarp();
+        rk[s] = base + __popc(peers & lanemask_lt());
+    }
+    __syncthreads();
+    {
+        uint32_t run = 0;
+#pragma unroll
+        for (int w = 0; w < kSortWarps; ++w) {
+            uint32_t c = wh[w][threadIdx.x];
+            wh[w][threadIdx.x] = run;
+            run += c;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int s = 0; s < kSortSteps; ++s) {
+        uint32_t d = dig[s];
+        if (d < 256) {
+            uint32_t pos = goff[d] + wh[warp][d] + rk[s];
+            kout[pos] = key[s];
+            if (vin) vout[pos] = val[s];
+        }
+    }
+}
+
+}  // namespace
+
+// Hierarchical scan: tile sums are scanned recursively in scan_tmp (used as a stack from
+// word `tmp_off` on), then every tile is rescanned with its offset.
+static int scan_level(kt_engine* e, const uint32_t* in, uint32_t* out, uint64_t n, uint64_t tmp_off) {
+    if (n == 0) return KT_OK;
+    if (n <= kScanTile) {
+        k_scan_tiles<<<1, kScanThreads, 0, e->stream>>>(in, out, n, nullptr);
+        count_launch(e);
+        return check_launch(e, "k_scan_tiles");
+    }
+    const uint64_t nb = (n + kScanTile - 1) / kScanTile;
+    const uint64_t words = (nb + 63) & ~63ull;
+    if (tmp_off + words > e->scan_tmp_words)
+        return fail(KT_ERR_INVALID_ARG, "scan scratch too small (%llu words)", (unsigned long long)e->scan_tmp_words);
+    uint32_t* sums = e->scan_tmp + tmp_off;
+    k_scan_tile_sums<<<(uint32_t)nb, kScanThreads, 0, e->stream>>>(in, n, sums);
+    count_launch(e);
+    int rc = check_launch(e, "k_scan_tile_sums");
+    if (rc) return rc;
+    rc = scan_level(e, sums, sums, nb, tmp_off + words);
+    if (rc) return rc;
+    k_scan_tiles<<<(uint32_t)nb, kScanThreads, 0, e->stream>>>(in, out, n, sums);
+    count_launch(e);
+    return check_launch(e, "k_scan_tiles");
+}
+
+int exclusive_scan(kt_engine* e, const uint32_t* in, uint32_t* out, uint64_t n) {
+    return scan_level(e, in, out, n, 0);
+}
+
+int radix_sort(kt_engine* e, uint64_t* key_a, uint32_t* val_a, uint64_t* key_b, uint32_t* val_b, uint64_t n,
+               unsigned bits, int* result_in_b) {
+    *result_in_b = 0;
+    if (n <= 1 || bits == 0) return KT_OK;
+    const uint64_t nb64 = (n + kSortTile - 1) / kSortTile;
+    if (nb64 * 256 > e->hist_words) return fail(KT_ERR_INVALID_ARG, "sort histogram scratch too small");
+    const uint32_t nb = (uint32_t)nb64;
+    uint64_t *kin = key_a, *kout = key_b;
+    uint32_t *vin = val_a, *vout = val_b;
+    for (unsigned shift = 0; shift < bits; shift += 8) {
+        k_radix_hist<<<nb, kSortThreads, 0, e->stream>>>(kin, n, shift, e->hist, nb);
+        count_launch(e);
+        int rc = check_launch(e, "k_radix_hist");
+        if (rc) return rc;
+        rc = exclusive_scan(e, e->hist, e->hist, (uint64_t)nb * 256);
+        if (rc) return rc;
+        k_radix_scatter<<<nb, kSortThreads, 0, e->stream>>>(kin, vin, kout, vout, n, shift, e->hist, nb);
+        count_launch(e);
+        rc = check_launch(e, "k_radix_scatter");
+        if (rc) return rc;
+        uint64_t* tk = kin; kin = kout; kout = tk;
+        uint32_t* tv = vin; vin = vout; vout = tv;
+        *result_in_b ^= 1;
+    }
+    return KT_OK;
+}
+
+}  // namespace kt

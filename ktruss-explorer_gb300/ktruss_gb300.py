@@ -1,0 +1,370 @@
+"""Python binding of libktruss_gb300 (ctypes over the C ABI in include/ktruss_gb300.h).
+
+Mirrors the reference's k-truss interface:
+    parse_args(argv)                  config.h:183-224   parseArgs
+    create_coo_from_file(path)        graph.cu:37-79     createCOOFromFile
+    write_coo_graph_to_file(g, path)  graph.cu:96-104    writeCOOGraphToFile
+    ktruss(graph, config)             kernel.h:12        ktruss (returns the truss graph)
+    verify(truss, config)             verify.cu:12-40    verify (raises KtrussError on mismatch)
+and adds decompose() (per-edge truss numbers, k_max), the device-resident Engine and the
+seeded generators.  Every call goes to the compiled library; there is no Python fallback:
+if the library is missing, importing fails with the build command to run.
+"""
+from __future__ import annotations
+
+import ctypes
+import dataclasses
+import os
+from typing import Optional
+
+import numpy as np
+
+PKG_DIR = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG_DIR, "lib", "libktruss_gb300.so")
+CLI_PATH = os.path.join(PKG_DIR, "bin", "ktruss")
+
+PROCESSOR = {"cpu": 0, "gpu": 1}
+DIRECTEDNESS = {"undirected": 0, "directed-by-index": 1, "directed-by-degree": 2}
+INPUT_FORMAT = {"coocsr": 0, "tiled-coocsr": 1}
+RECOUNT = {"all": 0, "affected": 1}
+
+KT_OK = 0
+STATUS_NAMES = {0: "KT_OK", 1: "KT_ERR_INVALID_ARG", 2: "KT_ERR_SELF_LOOP", 3: "KT_ERR_NOT_SYMMETRIC",
+                4: "KT_ERR_CAPACITY", 5: "KT_ERR_UNSUPPORTED", 6: "KT_ERR_CUDA", 7: "KT_ERR_DEVICE_ALLOC",
+                8: "KT_ERR_HOST_ALLOC", 9: "KT_ERR_IO", 10: "KT_ERR_MISMATCH", 11: "KT_ERR_TIMEOUT",
+                12: "KT_ERR_NO_DEVICE", 13: "KT_ERR_TOO_LARGE"}
+
+
+class KtrussError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {message}")
+        self.status = status
+
+
+class _Coo(ctypes.Structure):
+    _fields_ = [("num_nodes", ctypes.c_uint32), ("num_edges", ctypes.c_uint32), ("capacity", ctypes.c_uint32),
+                ("src_idx", ctypes.POINTER(ctypes.c_uint32)), ("dst_idx", ctypes.POINTER(ctypes.c_uint32))]
+
+
+class _Config(ctypes.Structure):
+    _fields_ = [("graph_file_name", ctypes.c_char_p), ("k", ctypes.c_uint32), ("compare_file_name", ctypes.c_char_p),
+                ("out_file_name", ctypes.c_char_p), ("num_warmup_runs", ctypes.c_uint32),
+                ("num_timed_runs", ctypes.c_uint32), ("processor", ctypes.c_int32), ("directedness", ctypes.c_int32),
+                ("input_format", ctypes.c_int32), ("num_edge_remove_iter", ctypes.c_uint32),
+                ("recount", ctypes.c_int32), ("block_size", ctypes.c_uint32), ("num_tiles", ctypes.c_uint32),
+                ("num_parallel_tiles", ctypes.c_uint32), ("verbosity", ctypes.c_uint32),
+                ("num_nodes", ctypes.c_uint32), ("num_edges", ctypes.c_uint32)]
+
+
+class _Edges(ctypes.Structure):
+    _fields_ = [("num_nodes", ctypes.c_uint32), ("num_edges", ctypes.c_uint64),
+                ("u", ctypes.POINTER(ctypes.c_uint32)), ("v", ctypes.POINTER(ctypes.c_uint32))]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("num_nodes", ctypes.c_uint32), ("num_edges", ctypes.c_uint64), ("k_max", ctypes.c_uint32),
+                ("num_levels", ctypes.c_uint32), ("num_rounds", ctypes.c_uint32), ("triangles", ctypes.c_uint64),
+                ("plain_alive_sum", ctypes.c_uint64), ("plain_passes", ctypes.c_uint32),
+                ("kernel_launches", ctypes.c_uint64), ("last_ms", ctypes.c_float),
+                ("build_ms", ctypes.c_float), ("support_ms", ctypes.c_float), ("peel_ms", ctypes.c_float)]
+
+    def as_dict(self) -> dict:
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+_LIB = None
+_U32P = ctypes.POINTER(ctypes.c_uint32)
+_VP = ctypes.c_void_p
+
+
+def lib() -> ctypes.CDLL:
+    """Loads libktruss_gb300.so (built by ktruss-explorer_gb300/build.py)."""
+    global _LIB
+    if _LIB is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing: run `python ktruss-explorer_gb300/build.py` "
+                              "(or __graft_entry__.build()) to compile the CUDA library")
+        L = ctypes.CDLL(LIB_PATH)
+        L.kt_last_error.restype = ctypes.c_char_p
+        L.kt_status_string.restype = ctypes.c_char_p
+        L.kt_status_string.argtypes = [ctypes.c_int]
+        L.kt_config_default.argtypes = [ctypes.POINTER(_Config)]
+        L.kt_parse_args.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(_Config)]
+        L.kt_coo_alloc.argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(_Coo)]
+        L.kt_coo_free.argtypes = [ctypes.POINTER(_Coo)]
+        L.kt_coo_free.restype = None
+        L.kt_read_tsv.argtypes = [ctypes.c_char_p, ctypes.POINTER(_Coo)]
+        L.kt_write_tsv.argtypes = [ctypes.POINTER(_Coo), ctypes.c_char_p]
+        L.kt_write_truss_tsv.argtypes = [ctypes.POINTER(_Coo), _U32P, ctypes.c_char_p]
+        L.kt_ktruss.argtypes = [ctypes.POINTER(_Coo), ctypes.POINTER(_Coo), ctypes.POINTER(_Config)]
+        L.kt_decompose.argtypes = [ctypes.POINTER(_Coo), _U32P, _U32P, ctypes.POINTER(_Config)]
+        L.kt_verify.argtypes = [ctypes.POINTER(_Coo), ctypes.POINTER(_Config)]
+        L.kt_engine_create.argtypes = [ctypes.c_int, ctypes.POINTER(_VP)]
+        L.kt_engine_destroy.argtypes = [_VP]
+        L.kt_engine_stream.argtypes = [_VP]
+        L.kt_engine_stream.restype = _VP
+        L.kt_engine_reserve.argtypes = [_VP, ctypes.c_uint32, ctypes.c_uint64]
+        L.kt_engine_decompose.argtypes = [_VP, _VP, _VP, ctypes.c_uint64, ctypes.c_uint32, _VP, _VP, ctypes.c_int]
+        L.kt_engine_ktruss.argtypes = [_VP, _VP, _VP, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32, _VP,
+                                       ctypes.c_int]
+        L.kt_engine_stats.argtypes = [_VP, ctypes.POINTER(Stats)]
+        for g in ("kt_gen_rmat",):
+            getattr(L, g).argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_double, ctypes.c_double,
+                                      ctypes.c_double, ctypes.c_uint64, ctypes.POINTER(_Edges)]
+        L.kt_gen_er.argtypes = [ctypes.c_uint32, ctypes.c_double, ctypes.c_uint64, ctypes.POINTER(_Edges)]
+        L.kt_gen_ba.argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint64, ctypes.POINTER(_Edges)]
+        L.kt_gen_ws.argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_double, ctypes.c_uint64,
+                                ctypes.POINTER(_Edges)]
+        L.kt_gen_rgg.argtypes = [ctypes.c_uint32, ctypes.c_double, ctypes.c_uint64, ctypes.POINTER(_Edges)]
+        L.kt_plant_cliques.argtypes = [ctypes.c_uint32, _U32P, _U32P, ctypes.c_uint64, ctypes.c_uint32,
+                                       ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint64, ctypes.POINTER(_Edges)]
+        L.kt_edges_free.argtypes = [ctypes.POINTER(_Edges)]
+        L.kt_edges_free.restype = None
+        _LIB = L
+    return _LIB
+
+
+def _check(rc: int) -> None:
+    if rc != KT_OK:
+        raise KtrussError(rc, lib().kt_last_error().decode(errors="replace"))
+
+
+# ---- configuration (config.h) -------------------------------------------------------------
+
+@dataclasses.dataclass
+class Config:
+    """Fields and defaults of the reference's Config (config.h:163-199)."""
+    graph_file_name: str = "data/loc-gowalla_edges_adj.tsv"
+    k: int = 3
+    compare_file_name: str = "data/loc-gowalla_edges_adj.tsv.3.reference.tsv"
+    out_file_name: Optional[str] = None
+    num_warmup_runs: int = 0
+    num_timed_runs: int = 1
+    processor: str = "gpu"
+    directedness: str = "directed-by-degree"
+    input_format: str = "coocsr"
+    num_edge_remove_iter: int = 0
+    recount: str = "all"
+    block_size: int = 512
+    num_tiles: int = 8
+    num_parallel_tiles: int = 8
+    verbosity: int = 1
+    num_nodes: int = 0
+    num_edges: int = 0
+
+    def _c(self) -> tuple[_Config, list]:
+        keep = [s.encode() if s is not None else None for s in
+                (self.graph_file_name, self.compare_file_name, self.out_file_name)]
+        c = _Config(keep[0], self.k & 0xFFFFFFFF, keep[1], keep[2], self.num_warmup_runs, self.num_timed_runs,
+                    PROCESSOR[self.processor], DIRECTEDNESS[self.directedness], INPUT_FORMAT[self.input_format],
+                    self.num_edge_remove_iter, RECOUNT[self.recount], self.block_size, self.num_tiles,
+                    self.num_parallel_tiles, self.verbosity, self.num_nodes, self.num_edges)
+        return c, keep
+
+
+def parse_args(argv: list[str]) -> Config:
+    """getopt parsing of the reference's flags; raises KtrussError on a bad option."""
+    args = [a.encode() for a in (["ktruss"] + list(argv))]
+    arr = (ctypes.c_char_p * len(args))(*args)
+    c = _Config()
+    _check(lib().kt_parse_args(len(args), arr, ctypes.byref(c)))
+    inv = lambda d, v: next(k for k, x in d.items() if x == v)
+    return Config(c.graph_file_name.decode(), c.k, c.compare_file_name.decode(),
+                  c.out_file_name.decode() if c.out_file_name else None, c.num_warmup_runs, c.num_timed_runs,
+                  inv(PROCESSOR, c.processor), inv(DIRECTEDNESS, c.directedness), inv(INPUT_FORMAT, c.input_format),
+                  c.num_edge_remove_iter, inv(RECOUNT, c.recount), c.block_size, c.num_tiles, c.num_parallel_tiles,
+                  c.verbosity, c.num_nodes, c.num_edges)
+
+
+# ---- graphs (graph.h COOGraph) --------------------------------------------------------------
+
+@dataclasses.dataclass
+class COOGraph:
+    """COOGraph (graph.h:10-16): every undirected edge once per direction, 0-based ids."""
+    num_nodes: int
+    src_idx: np.ndarray
+    dst_idx: np.ndarray
+
+    def __post_init__(self):
+        self.src_idx = np.ascontiguousarray(self.src_idx, dtype=np.uint32)
+        self.dst_idx = np.ascontiguousarray(self.dst_idx, dtype=np.uint32)
+        if self.src_idx.shape != self.dst_idx.shape:
+            raise ValueError("src_idx and dst_idx differ in length")
+
+    @property
+    def num_edges(self) -> int:
+        return int(self.src_idx.size)
+
+    def _c(self) -> _Coo:
+        return _Coo(self.num_nodes, self.num_edges, self.num_edges, self.src_idx.ctypes.data_as(_U32P),
+                    self.dst_idx.ctypes.data_as(_U32P))
+
+    @staticmethod
+    def from_undirected(num_nodes: int, u, v) -> "COOGraph":
+        """Both directions of each undirected edge (u[i], v[i])."""
+        u = np.asarray(u, dtype=np.uint32)
+        v = np.asarray(v, dtype=np.uint32)
+        return COOGraph(num_nodes, np.concatenate([u, v]), np.concatenate([v, u]))
+
+    def canonical(self) -> np.ndarray:
+        """Sorted unique (min, max) pairs as uint64 keys."""
+        a = np.minimum(self.src_idx, self.dst_idx).astype(np.uint64)
+        b = np.maximum(self.src_idx, self.dst_idx).astype(np.uint64)
+        return np.unique((a << np.uint64(32)) | b)
+
+
+def _from_c(c: _Coo) -> COOGraph:
+    n = c.num_edges
+    s = np.ctypeslib.as_array(c.src_idx, shape=(n,)).copy() if n else np.zeros(0, np.uint32)
+    d = np.ctypeslib.as_array(c.dst_idx, shape=(n,)).copy() if n else np.zeros(0, np.uint32)
+    return COOGraph(c.num_nodes, s, d)
+
+
+def create_coo_from_file(path: str) -> COOGraph:
+    c = _Coo()
+    _check(lib().kt_read_tsv(path.encode(), ctypes.byref(c)))
+    try:
+        return _from_c(c)
+    finally:
+        lib().kt_coo_free(ctypes.byref(c))
+
+
+def write_coo_graph_to_file(graph: COOGraph, path: str) -> None:
+    c = graph._c()
+    _check(lib().kt_write_tsv(ctypes.byref(c), path.encode()))
+
+
+def write_truss_to_file(graph: COOGraph, truss_per_entry: np.ndarray, path: str) -> None:
+    t = np.ascontiguousarray(truss_per_entry, dtype=np.uint32)
+    c = graph._c()
+    _check(lib().kt_write_truss_tsv(ctypes.byref(c), t.ctypes.data_as(_U32P), path.encode()))
+
+
+# ---- the k-truss path -----------------------------------------------------------------------
+
+def ktruss(graph: COOGraph, config: Optional[Config] = None) -> COOGraph:
+    """k-truss for config.k on the GPU (kernel.h:12); returns the truss in both directions."""
+    config = config or Config()
+    cfg, _keep = config._c()
+    cfg.num_nodes, cfg.num_edges = graph.num_nodes, graph.num_edges
+    g = graph._c()
+    out_s = np.empty(max(graph.num_edges, 1), np.uint32)
+    out_d = np.empty(max(graph.num_edges, 1), np.uint32)
+    t = _Coo(graph.num_nodes, 0, graph.num_edges, out_s.ctypes.data_as(_U32P), out_d.ctypes.data_as(_U32P))
+    _check(lib().kt_ktruss(ctypes.byref(g), ctypes.byref(t), ctypes.byref(cfg)))
+    return COOGraph(t.num_nodes, out_s[: t.num_edges].copy(), out_d[: t.num_edges].copy())
+
+
+def decompose(graph: COOGraph, config: Optional[Config] = None,
+              out: Optional[np.ndarray] = None) -> tuple[np.ndarray, int]:
+    """Per-entry truss numbers and k_max on the GPU.  `out` (uint32, num_edges) may be a
+    caller-owned (for example pinned) buffer to receive the result."""
+    g = graph._c()
+    if out is None:
+        out = np.zeros(max(graph.num_edges, 1), np.uint32)
+    elif out.dtype != np.uint32 or not out.flags.c_contiguous or out.size < graph.num_edges:
+        raise ValueError("out must be a contiguous uint32 array with num_edges elements")
+    kmax = ctypes.c_uint32(0)
+    cfg = None
+    keep = None
+    if config is not None:
+        cfg, keep = config._c()
+    _check(lib().kt_decompose(ctypes.byref(g), out.ctypes.data_as(_U32P), ctypes.byref(kmax),
+                              ctypes.byref(cfg) if cfg is not None else None))
+    del keep
+    return out[: graph.num_edges], kmax.value
+
+
+def verify(truss: COOGraph, config: Config) -> None:
+    """verify.cu:12-40: raises KtrussError(KT_ERR_MISMATCH) if the edge sets differ."""
+    cfg, _keep = config._c()
+    t = truss._c()
+    _check(lib().kt_verify(ctypes.byref(t), ctypes.byref(cfg)))
+
+
+class Engine:
+    """Device-resident engine: graph and outputs stay in HBM (pointers are device addresses)."""
+
+    def __init__(self, device: int = 0):
+        h = _VP()
+        _check(lib().kt_engine_create(device, ctypes.byref(h)))
+        self._h = h
+
+    def close(self) -> None:
+        if self._h:
+            lib().kt_engine_destroy(self._h)
+            self._h = _VP()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def stream(self) -> int:
+        return lib().kt_engine_stream(self._h) or 0
+
+    def reserve(self, max_nodes: int, max_entries: int) -> None:
+        _check(lib().kt_engine_reserve(self._h, max_nodes, max_entries))
+
+    def decompose(self, d_src: int, d_dst: int, num_entries: int, num_nodes: int, d_truss: int,
+                  d_k_max: int = 0, sync: bool = True) -> None:
+        _check(lib().kt_engine_decompose(self._h, d_src, d_dst, num_entries, num_nodes, d_truss, d_k_max or None,
+                                         int(sync)))
+
+    def ktruss(self, d_src: int, d_dst: int, num_entries: int, num_nodes: int, k: int, d_keep: int,
+               sync: bool = True) -> None:
+        _check(lib().kt_engine_ktruss(self._h, d_src, d_dst, num_entries, num_nodes, k & 0xFFFFFFFF, d_keep,
+                                      int(sync)))
+
+    def stats(self) -> Stats:
+        s = Stats()
+        _check(lib().kt_engine_stats(self._h, ctypes.byref(s)))
+        return s
+
+
+# ---- generators -----------------------------------------------------------------------------
+
+def _edges(fn, *args) -> tuple[int, np.ndarray, np.ndarray]:
+    e = _Edges()
+    _check(fn(*args, ctypes.byref(e)))
+    try:
+        n = e.num_edges
+        u = np.ctypeslib.as_array(e.u, shape=(n,)).copy() if n else np.zeros(0, np.uint32)
+        v = np.ctypeslib.as_array(e.v, shape=(n,)).copy() if n else np.zeros(0, np.uint32)
+        return e.num_nodes, u, v
+    finally:
+        lib().kt_edges_free(ctypes.byref(e))
+
+
+def gen_rmat(scale: int, edge_factor: int, a=0.57, b=0.19, c=0.19, seed: int = 1):
+    return _edges(lib().kt_gen_rmat, scale, edge_factor, a, b, c, seed)
+
+
+def gen_er(n: int, p: float, seed: int = 1):
+    return _edges(lib().kt_gen_er, n, p, seed)
+
+
+def gen_ba(n: int, m: int, seed: int = 1):
+    return _edges(lib().kt_gen_ba, n, m, seed)
+
+
+def gen_ws(n: int, k: int, p: float, seed: int = 1):
+    return _edges(lib().kt_gen_ws, n, k, p, seed)
+
+
+def gen_rgg(n: int, radius: float, seed: int = 1):
+    return _edges(lib().kt_gen_rgg, n, radius, seed)
+
+
+def plant_cliques(num_nodes: int, u: np.ndarray, v: np.ndarray, count: int, min_size: int, max_size: int,
+                  seed: int = 1):
+    u = np.ascontiguousarray(u, dtype=np.uint32)
+    v = np.ascontiguousarray(v, dtype=np.uint32)
+    return _edges(lib().kt_plant_cliques, num_nodes, u.ctypes.data_as(_U32P), v.ctypes.data_as(_U32P), u.size,
+                  count, min_size, max_size, seed)
+
+
+def coo_from_edges(num_nodes: int, u: np.ndarray, v: np.ndarray) -> COOGraph:
+    return COOGraph.from_undirected(num_nodes, u, v)

@@ -1,0 +1,117 @@
+"""TEST INFRASTRUCTURE ONLY: ctypes bindings of the CPU oracle (ktruss_oracle.c).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use this module, as the
+checker or the timed CPU baseline.  The product library never loads it.
+
+Graphs are numpy uint32 arrays ``src``/``dst`` holding every undirected edge once per
+direction (the COO convention of the reference, graph.h:10-16).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libktoracle.so")
+
+UNDIRECTED, DIRECTED_BY_INDEX, DIRECTED_BY_DEGREE = 0, 1, 2
+RECOUNT_ALL, RECOUNT_AFFECTED = 0, 1
+
+_lib = None
+
+
+class _PassLog(ctypes.Structure):
+    _fields_ = [("cap", ctypes.c_uint32), ("num", ctypes.c_uint32), ("alive", ctypes.POINTER(ctypes.c_uint64))]
+
+
+def build() -> str:
+    """Compiles oracle/_build/libktoracle.so with the committed Makefile."""
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+    return LIB_PATH
+
+
+def _load():
+    global _lib
+    if _lib is None:
+        src = os.path.join(HERE, "ktruss_oracle.c")
+        if not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < os.path.getmtime(src):
+            build()
+        lib = ctypes.CDLL(LIB_PATH)
+        u32p = ctypes.POINTER(ctypes.c_uint32)
+        lib.ko_ktruss.argtypes = [ctypes.c_uint32, ctypes.c_uint32, u32p, u32p, ctypes.c_uint32, ctypes.c_int,
+                                  ctypes.c_int, ctypes.c_uint32, u32p, u32p, u32p, ctypes.POINTER(_PassLog)]
+        lib.ko_decompose_chain.argtypes = [ctypes.c_uint32, ctypes.c_uint32, u32p, u32p, u32p, u32p, u32p,
+                                           ctypes.POINTER(ctypes.c_uint64)]
+        lib.ko_chain_sample.argtypes = [ctypes.c_uint32, ctypes.c_uint32, u32p, u32p, ctypes.c_double, u32p,
+                                        ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_double)]
+        lib.ko_decompose_peel.argtypes = [ctypes.c_uint32, ctypes.c_uint32, u32p, u32p, u32p, u32p, u32p,
+                                          ctypes.POINTER(ctypes.c_uint64), u32p]
+        _lib = lib
+    return _lib
+
+
+def _p(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32))
+
+
+def _u32(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.uint32)
+
+
+def ktruss(num_nodes: int, src, dst, k: int, directedness: int = DIRECTED_BY_DEGREE,
+           recount: int = RECOUNT_ALL, num_edge_remove_iter: int = 0, pass_log: bool = False):
+    """Single-k k-truss (the reference's Host path).  Returns (out_src, out_dst[, alive per pass])."""
+    lib = _load()
+    src, dst = _u32(src), _u32(dst)
+    n = len(src)
+    os_, od = np.zeros(max(n, 1), np.uint32), np.zeros(max(n, 1), np.uint32)
+    num = ctypes.c_uint32(0)
+    alive = np.zeros(1 << 16, np.uint64)
+    log = _PassLog(len(alive), 0, alive.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)))
+    rc = lib.ko_ktruss(num_nodes, n, _p(src), _p(dst), k & 0xFFFFFFFF, directedness, recount,
+                       num_edge_remove_iter, _p(os_), _p(od), ctypes.byref(num), ctypes.byref(log))
+    if rc != 0:
+        raise MemoryError("oracle ko_ktruss failed")
+    out = (os_[: num.value].copy(), od[: num.value].copy())
+    if pass_log:
+        return out + (alive[: min(log.num, len(alive))].copy(),)
+    return out
+
+
+def decompose(num_nodes: int, src, dst, method: str = "peel"):
+    """Per-entry truss numbers.  method 'chain' chains single-k runs like the reference
+    would be driven; 'peel' is the exact serial peeling.  Returns a dict."""
+    lib = _load()
+    src, dst = _u32(src), _u32(dst)
+    n = len(src)
+    truss = np.zeros(max(n, 1), np.uint32)
+    kmax, passes, rounds = ctypes.c_uint32(0), ctypes.c_uint32(0), ctypes.c_uint32(0)
+    alive_sum = ctypes.c_uint64(0)
+    if method == "chain":
+        rc = lib.ko_decompose_chain(num_nodes, n, _p(src), _p(dst), _p(truss), ctypes.byref(kmax),
+                                    ctypes.byref(passes), ctypes.byref(alive_sum))
+    elif method == "peel":
+        rc = lib.ko_decompose_peel(num_nodes, n, _p(src), _p(dst), _p(truss), ctypes.byref(kmax),
+                                   ctypes.byref(passes), ctypes.byref(alive_sum), ctypes.byref(rounds))
+    else:
+        raise ValueError(method)
+    if rc != 0:
+        raise MemoryError("oracle decomposition failed")
+    return {"truss": truss[:n].copy(), "k_max": kmax.value, "plain_passes": passes.value,
+            "plain_alive_sum": alive_sum.value, "rounds": rounds.value if method == "peel" else None}
+
+
+def chain_sample(num_nodes: int, src, dst, budget_s: float) -> dict:
+    """Times the reference algorithm (chained count-and-prune passes) for about budget_s
+    seconds; returns the passes completed, their summed alive edges and the seconds taken."""
+    lib = _load()
+    src, dst = _u32(src), _u32(dst)
+    passes, alive, secs = ctypes.c_uint32(0), ctypes.c_uint64(0), ctypes.c_double(0)
+    rc = lib.ko_chain_sample(num_nodes, len(src), _p(src), _p(dst), budget_s, ctypes.byref(passes),
+                             ctypes.byref(alive), ctypes.byref(secs))
+    if rc != 0:
+        raise MemoryError("oracle chain sample failed")
+    return {"passes": passes.value, "alive_sum": alive.value, "seconds": secs.value}

@@ -1,0 +1,158 @@
+"""GPU parity: the CUDA engine through the C ABI against the golden fixtures and the oracle.
+
+Bar: bit-exact truss numbers, k_max and k-truss edge sets."""
+import hashlib
+
+import numpy as np
+import pytest
+
+import ktruss_gb300 as kt
+import oracle
+from conftest import GOLDEN_NAMES, both_directions, edge_keys, load_golden
+
+pytestmark = pytest.mark.gpu
+
+
+def sha_of_keys(keys):
+    if len(keys) == 0:
+        return "empty"
+    u = (keys >> np.uint64(32)).astype(np.uint32)
+    v = (keys & np.uint64(0xFFFFFFFF)).astype(np.uint32)
+    return hashlib.sha256(np.stack([u, v], 1).astype("<u4").tobytes()).hexdigest()
+
+
+@pytest.mark.parametrize("name", GOLDEN_NAMES)
+def test_decompose_matches_golden(name, manifest):
+    n, u, v, t = load_golden(name)
+    src, dst = both_directions(u, v)
+    truss, k_max = kt.decompose(kt.COOGraph(n, src, dst))
+    assert k_max == manifest["graphs"][name]["k_max"]
+    assert np.array_equal(truss[: len(u)], t)
+    assert np.array_equal(truss[len(u):], t)
+
+
+CONFIGS = [dict(), dict(directedness="undirected"), dict(directedness="directed-by-index"),
+           dict(recount="affected"), dict(num_edge_remove_iter=1), dict(input_format="tiled-coocsr", num_tiles=4),
+           dict(block_size=128)]
+
+
+@pytest.mark.parametrize("name", GOLDEN_NAMES)
+def test_single_k_matches_golden(name, manifest):
+    n, u, v, t = load_golden(name)
+    src, dst = both_directions(u, v)
+    g = kt.COOGraph(n, src, dst)
+    for k_str, chk in manifest["graphs"][name]["single_k"].items():
+        for cfg in CONFIGS:
+            out = kt.ktruss(g, kt.Config(k=int(k_str), verbosity=1, **cfg))
+            keys = edge_keys(out.src_idx, out.dst_idx)
+            assert out.num_edges == 2 * len(keys)
+            assert len(keys) == chk["edges"], (k_str, cfg)
+            assert sha_of_keys(keys) == chk["sha"], (k_str, cfg)
+
+
+GENERATED = [
+    ("rmat14", lambda: kt.gen_rmat(14, 16, 0.57, 0.19, 0.19, 3)),
+    ("rmat16_ef8", lambda: kt.gen_rmat(16, 8, 0.57, 0.19, 0.19, 4)),
+    ("ba20000", lambda: kt.plant_cliques(*kt.gen_ba(20000, 8, 5), 3, 20, 64, 9)),
+    ("ws20000", lambda: kt.gen_ws(20000, 20, 0.1, 6)),
+    ("rgg20000", lambda: kt.gen_rgg(20000, 0.02, 7)),
+    ("er8192_cliques", lambda: kt.plant_cliques(*kt.gen_er(8192, 0.002, 8), 4, 30, 90, 10)),
+]
+
+
+@pytest.mark.parametrize("name,make", GENERATED, ids=[g[0] for g in GENERATED])
+def test_decompose_matches_oracle(name, make):
+    n, u, v = make()
+    src, dst = both_directions(u, v)
+    truss, k_max = kt.decompose(kt.COOGraph(n, src, dst))
+    ref = oracle.decompose(n, src, dst, method="peel")
+    assert k_max == ref["k_max"]
+    assert np.array_equal(truss, ref["truss"])
+
+
+def test_engine_stats_match_reference_pass_accounting():
+    """The engine's round log reproduces the reference loop's pass statistics."""
+    torch = pytest.importorskip("torch")
+    n, u, v = kt.gen_rmat(12, 16, 0.57, 0.19, 0.19, 2)
+    src, dst = both_directions(u, v)
+    ref = oracle.decompose(n, src, dst, method="peel")
+    eng = kt.Engine(0)
+    d_src = torch.from_numpy(src.view(np.int32)).cuda()
+    d_dst = torch.from_numpy(dst.view(np.int32)).cuda()
+    d_out = torch.zeros(len(src), dtype=torch.int32, device="cuda")
+    d_k = torch.zeros(1, dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    eng.decompose(d_src.data_ptr(), d_dst.data_ptr(), len(src), n, d_out.data_ptr(), d_k.data_ptr())
+    s = eng.stats()
+    assert int(d_k.item()) == ref["k_max"] == s.k_max
+    assert np.array_equal(d_out.cpu().numpy().view(np.uint32), ref["truss"])
+    assert s.plain_passes == ref["plain_passes"]
+    assert s.plain_alive_sum == ref["plain_alive_sum"]
+    assert s.num_rounds == ref["rounds"]
+    assert s.num_edges == len(u)
+    eng.close()
+
+
+def test_repeated_calls_are_stable():
+    n, u, v = kt.gen_rmat(11, 16, 0.57, 0.19, 0.19, 5)
+    g = kt.COOGraph.from_undirected(n, u, v)
+    a, ka = kt.decompose(g)
+    b, kb = kt.decompose(g)
+    assert ka == kb and np.array_equal(a, b)
+
+
+# ---- error behaviour (the reference asserts; here statuses) --------------------------------
+
+def test_self_loop_rejected():
+    g = kt.COOGraph(3, np.array([0, 1, 1, 2, 2], np.uint32), np.array([1, 0, 2, 1, 2], np.uint32))
+    with pytest.raises(kt.KtrussError) as ei:
+        kt.decompose(g)
+    assert ei.value.status == 2
+
+
+def test_asymmetric_rejected():
+    g = kt.COOGraph(3, np.array([0, 1, 1, 2], np.uint32), np.array([1, 0, 2, 0], np.uint32))
+    with pytest.raises(kt.KtrussError) as ei:
+        kt.decompose(g)
+    assert ei.value.status == 3
+
+
+def test_duplicate_rejected():
+    g = kt.COOGraph(3, np.array([0, 1, 0, 1], np.uint32), np.array([1, 0, 1, 0], np.uint32))
+    with pytest.raises(kt.KtrussError) as ei:
+        kt.decompose(g)
+    assert ei.value.status == 3
+
+
+def test_bad_vertex_rejected():
+    g = kt.COOGraph(2, np.array([0, 5], np.uint32), np.array([5, 0], np.uint32))
+    with pytest.raises(kt.KtrussError) as ei:
+        kt.decompose(g)
+    assert ei.value.status == 1
+
+
+def test_empty_graph():
+    g = kt.COOGraph(0, np.zeros(0, np.uint32), np.zeros(0, np.uint32))
+    truss, k_max = kt.decompose(g)
+    assert len(truss) == 0 and k_max == 0
+    out = kt.ktruss(g, kt.Config(k=3))
+    assert out.num_edges == 0
+
+
+def test_isolated_vertices_and_large_k():
+    n, u, v, t = load_golden("tiny9")
+    src, dst = both_directions(u, v)
+    g = kt.COOGraph(50, src, dst)  # vertices 9..49 isolated
+    truss, k_max = kt.decompose(g)
+    assert k_max == 5 and np.array_equal(truss[: len(u)], t)
+    for k in (6, 100, 2**31, 2**32 - 1):
+        assert kt.ktruss(g, kt.Config(k=k)).num_edges == 0
+
+
+def test_engine_after_error_still_usable():
+    bad = kt.COOGraph(3, np.array([0, 1, 1, 2], np.uint32), np.array([1, 0, 2, 0], np.uint32))
+    with pytest.raises(kt.KtrussError):
+        kt.decompose(bad)
+    n, u, v, t = load_golden("k6")
+    truss, k_max = kt.decompose(kt.COOGraph.from_undirected(n, u, v))
+    assert k_max == 6
