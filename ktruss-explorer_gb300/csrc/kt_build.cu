@@ -25,6 +25,7 @@ namespace kt {
 namespace {
 
 constexpr int kThreads = 256;
+constexpr uint32_t kBigRow = 2048;  // rows this long are compacted by a whole block
 
 inline uint32_t grid_for(uint64_t n, int threads = kThreads) {
     uint64_t b = (n + threads - 1) / threads;
@@ -151,6 +152,24 @@ __global__ void k_in_eid(const uint64_t* __restrict__ keys, uint64_t entries, un
     if (err && lane_id() == 0) atomicOr(&ctrl[kCtrlError], err);
 }
 
+// First rank whose symmetric row has at least `thr` entries (rows grow with rank: ranks are
+// ascending degree), written to ctrl[kCtrlBigRow].
+__global__ void k_find_big_row(const uint32_t* __restrict__ s_ptr, uint32_t n, uint32_t thr,
+                               uint32_t* __restrict__ ctrl) {
+    uint32_t lo = 0, len = n;
+    while (len > 0) {
+        uint32_t half = len >> 1;
+        uint32_t r = lo + half;
+        if (s_ptr[r + 1] - s_ptr[r] < thr) {
+            lo = r + 1;
+            len -= half + 1;
+        } else {
+            len = half;
+        }
+    }
+    ctrl[kCtrlBigRow] = lo;
+}
+
 unsigned bits_for(uint64_t n) {
     unsigned b = 1;
     while (b < 64 && (1ull << b) < n) ++b;
@@ -262,7 +281,12 @@ int build_graph(kt_engine* e, const uint32_t* d_src, const uint32_t* d_dst, uint
         count_launch(e);
         if ((rc = check_launch(e, "k_in_eid"))) return rc;
     }
-    return sync_and_check(e);
+    k_find_big_row<<<1, 1, 0, st>>>(e->s_ptr, n, kBigRow, e->ctrl);
+    count_launch(e);
+    if ((rc = check_launch(e, "k_find_big_row"))) return rc;
+    if ((rc = sync_and_check(e))) return rc;
+    e->big_row = e->h_ctrl[kCtrlBigRow];
+    return KT_OK;
 }
 
 }  // namespace kt

@@ -34,6 +34,9 @@ enum : uint32_t {
     kCtrlBarrierGen = 9,  // grid barrier generation
     kCtrlTriLo = 10,      // 64-bit triangle counter (lo, hi)
     kCtrlTriHi = 11,
+    kCtrlItems0 = 12,     // work-item queue counters
+    kCtrlItems1 = 13,
+    kCtrlBigRow = 14,     // first rank whose symmetric row is long (block-wide compaction)
     kCtrlWords = 16,
 };
 

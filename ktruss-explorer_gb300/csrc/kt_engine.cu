@@ -48,7 +48,8 @@ size_t carve(kt_engine* e, char* base, uint32_t n, uint64_t N) {
     const uint64_t sort_blocks = (keys + 2047) / 2048;
     const uint64_t hist_words = 256 * sort_blocks;
     const uint64_t scan_max = std::max<uint64_t>((uint64_t)n + 1, hist_words);
-    const uint64_t scan_words = scan_max / 4096 + 4096;
+    // u32 words; the u64 scan of the per-round work offsets (m+1 elements) uses it as u64
+    const uint64_t scan_words = 2 * (std::max<uint64_t>(scan_max, m + 1) / 4096 + 4096);
     Carver c{base};
     e->key_a = c.take<uint64_t>(keys);
     e->key_b = c.take<uint64_t>(keys);
@@ -71,6 +72,10 @@ size_t carve(kt_engine* e, char* base, uint32_t n, uint64_t N) {
     e->q1 = c.take<uint32_t>(m);
     e->alive0 = c.take<uint32_t>(m);
     e->alive1 = c.take<uint32_t>(m);
+    e->fx = c.take<uint32_t>(m);
+    e->fy = c.take<uint32_t>(m);
+    e->fbase = c.take<uint32_t>(m);
+    e->work = c.take<uint64_t>(m + 1);
     e->hist = c.take<uint32_t>(hist_words);
     e->hist_words = hist_words;
     e->scan_tmp = c.take<uint32_t>(scan_words);

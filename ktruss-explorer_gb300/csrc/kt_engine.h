@@ -47,6 +47,12 @@ struct kt_engine {
     uint32_t* q1 = nullptr;
     uint32_t* alive0 = nullptr;   // compacted lists of alive edge ids
     uint32_t* alive1 = nullptr;
+    // Per frontier slot: shorter endpoint, other endpoint, row start, and work offsets (u64).
+    uint32_t* fx = nullptr;
+    uint32_t* fy = nullptr;
+    uint32_t* fbase = nullptr;
+    uint64_t* work = nullptr;     // m+1
+    uint32_t big_row = 0;         // ranks >= big_row have rows of kBigRow entries or more
     // Scratch for scans and sort histograms.
     uint32_t* scan_tmp = nullptr;
     size_t scan_tmp_words = 0;
@@ -85,6 +91,7 @@ int reserve(kt_engine* e, uint32_t max_nodes, uint64_t max_entries);
 
 // kt_sort.cu
 int exclusive_scan(kt_engine* e, const uint32_t* in, uint32_t* out, uint64_t n);
+int exclusive_scan_u64(kt_engine* e, const uint64_t* in, uint64_t* out, uint64_t n);
 // Sorts (keys, vals) by the low `bits` bits of the keys; ping-pongs between a and b buffers
 // and returns 0 if the result is in (key_a, val_a), 1 if in (key_b, val_b).  vals may be null.
 int radix_sort(kt_engine* e, uint64_t* key_a, uint32_t* val_a, uint64_t* key_b, uint32_t* val_b,

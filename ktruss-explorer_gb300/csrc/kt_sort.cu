@@ -15,69 +15,72 @@ constexpr int kScanItems = 4;
 constexpr uint32_t kScanTile = kScanThreads * kScanItems;  // 4096
 
 // Block-wide exclusive scan of one value per thread; returns the block total in *total.
-__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* warp_sums, uint32_t* total) {
+template <class T>
+__device__ __forceinline__ T block_exclusive_scan(T v, T* warp_sums, T* total) {
     const uint32_t lane = lane_id(), warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-    uint32_t x = v;
+    T x = v;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-        uint32_t y = __shfl_up_sync(kFullMask, x, o);
+        T y = __shfl_up_sync(kFullMask, x, o);
         if (lane >= (uint32_t)o) x += y;
     }
     if (lane == 31) warp_sums[warp] = x;
     __syncthreads();
     if (warp == 0) {
-        uint32_t w = lane < nwarps ? warp_sums[lane] : 0;
-        uint32_t s = w;
+        T w = lane < nwarps ? warp_sums[lane] : T(0);
+        T s = w;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-            uint32_t y = __shfl_up_sync(kFullMask, s, o);
+            T y = __shfl_up_sync(kFullMask, s, o);
             if (lane >= (uint32_t)o) s += y;
         }
         if (lane < nwarps) warp_sums[lane] = s - w;
         if (lane == 31) warp_sums[32] = s;
     }
     __syncthreads();
-    uint32_t r = warp_sums[warp] + x - v;
+    T r = warp_sums[warp] + x - v;
     *total = warp_sums[32];
     __syncthreads();
     return r;
 }
 
-__global__ void __launch_bounds__(kScanThreads) k_scan_tile_sums(const uint32_t* __restrict__ in, uint64_t n,
-                                                                   uint32_t* __restrict__ sums) {
-    __shared__ uint32_t ws[33];
+template <class T>
+__global__ void __launch_bounds__(kScanThreads) k_scan_tile_sums(const T* __restrict__ in, uint64_t n,
+                                                                   T* __restrict__ sums) {
+    __shared__ T ws[33];
     const uint64_t base = (uint64_t)blockIdx.x * kScanTile;
-    uint32_t s = 0;
+    T s = 0;
 #pragma unroll
     for (int i = 0; i < kScanItems; ++i) {
         uint64_t idx = base + threadIdx.x + (uint64_t)i * kScanThreads;
         if (idx < n) s += in[idx];
     }
-    uint32_t total;
-    block_exclusive_scan(s, ws, &total);
+    T total;
+    block_exclusive_scan<T>(s, ws, &total);
     if (threadIdx.x == 0) sums[blockIdx.x] = total;
 }
 
 // Exclusive scan of each tile, offset by the scanned tile sums (if given).
-__global__ void __launch_bounds__(kScanThreads) k_scan_tiles(const uint32_t* in, uint32_t* out, uint64_t n,
-                                                               const uint32_t* __restrict__ tile_offsets) {
-    __shared__ uint32_t tile[kScanTile];
-    __shared__ uint32_t ws[33];
+template <class T>
+__global__ void __launch_bounds__(kScanThreads) k_scan_tiles(const T* in, T* out, uint64_t n,
+                                                               const T* __restrict__ tile_offsets) {
+    __shared__ T tile[kScanTile];
+    __shared__ T ws[33];
     const uint64_t base = (uint64_t)blockIdx.x * kScanTile;
 #pragma unroll
     for (int i = 0; i < kScanItems; ++i) {
         uint64_t idx = base + threadIdx.x + (uint64_t)i * kScanThreads;
-        tile[threadIdx.x + i * kScanThreads] = idx < n ? in[idx] : 0u;
+        tile[threadIdx.x + i * kScanThreads] = idx < n ? in[idx] : T(0);
     }
     __syncthreads();
-    uint32_t v[kScanItems], s = 0;
+    T v[kScanItems], s = 0;
 #pragma unroll
     for (int i = 0; i < kScanItems; ++i) {
         v[i] = tile[threadIdx.x * kScanItems + i];
         s += v[i];
     }
-    uint32_t total;
-    uint32_t run = block_exclusive_scan(s, ws, &total) + (tile_offsets ? tile_offsets[blockIdx.x] : 0u);
+    T total;
+    T run = block_exclusive_scan<T>(s, ws, &total) + (tile_offsets ? tile_offsets[blockIdx.x] : T(0));
 #pragma unroll
     for (int i = 0; i < kScanItems; ++i) {
         tile[threadIdx.x * kScanItems + i] = run;
@@ -169,33 +172,38 @@ __global__ void __launch_bounds__(kSortThreads) k_radix_scatter(const uint64_t* 
 
 }  // namespace
 
-// Hierarchical scan: tile sums are scanned recursively in scan_tmp (used as a stack from
+// Hierarchical scan: tile sums are scanned recursively in scratch (used as a stack from
 // word `tmp_off` on), then every tile is rescanned with its offset.
-static int scan_level(kt_engine* e, const uint32_t* in, uint32_t* out, uint64_t n, uint64_t tmp_off) {
+template <class T>
+static int scan_level(kt_engine* e, const T* in, T* out, uint64_t n, T* tmp, uint64_t tmp_words, uint64_t tmp_off) {
     if (n == 0) return KT_OK;
     if (n <= kScanTile) {
-        k_scan_tiles<<<1, kScanThreads, 0, e->stream>>>(in, out, n, nullptr);
+        k_scan_tiles<T><<<1, kScanThreads, 0, e->stream>>>(in, out, n, nullptr);
         count_launch(e);
         return check_launch(e, "k_scan_tiles");
     }
     const uint64_t nb = (n + kScanTile - 1) / kScanTile;
     const uint64_t words = (nb + 63) & ~63ull;
-    if (tmp_off + words > e->scan_tmp_words)
-        return fail(KT_ERR_INVALID_ARG, "scan scratch too small (%llu words)", (unsigned long long)e->scan_tmp_words);
-    uint32_t* sums = e->scan_tmp + tmp_off;
-    k_scan_tile_sums<<<(uint32_t)nb, kScanThreads, 0, e->stream>>>(in, n, sums);
+    if (tmp_off + words > tmp_words)
+        return fail(KT_ERR_INVALID_ARG, "scan scratch too small (%llu elements)", (unsigned long long)tmp_words);
+    T* sums = tmp + tmp_off;
+    k_scan_tile_sums<T><<<(uint32_t)nb, kScanThreads, 0, e->stream>>>(in, n, sums);
     count_launch(e);
     int rc = check_launch(e, "k_scan_tile_sums");
     if (rc) return rc;
-    rc = scan_level(e, sums, sums, nb, tmp_off + words);
+    rc = scan_level<T>(e, sums, sums, nb, tmp, tmp_words, tmp_off + words);
     if (rc) return rc;
-    k_scan_tiles<<<(uint32_t)nb, kScanThreads, 0, e->stream>>>(in, out, n, sums);
+    k_scan_tiles<T><<<(uint32_t)nb, kScanThreads, 0, e->stream>>>(in, out, n, sums);
     count_launch(e);
     return check_launch(e, "k_scan_tiles");
 }
 
 int exclusive_scan(kt_engine* e, const uint32_t* in, uint32_t* out, uint64_t n) {
-    return scan_level(e, in, out, n, 0);
+    return scan_level<uint32_t>(e, in, out, n, e->scan_tmp, e->scan_tmp_words, 0);
+}
+
+int exclusive_scan_u64(kt_engine* e, const uint64_t* in, uint64_t* out, uint64_t n) {
+    return scan_level<uint64_t>(e, in, out, n, reinterpret_cast<uint64_t*>(e->scan_tmp), e->scan_tmp_words / 2, 0);
 }
 
 int radix_sort(kt_engine* e, uint64_t* key_a, uint32_t* val_a, uint64_t* key_b, uint32_t* val_b, uint64_t n,

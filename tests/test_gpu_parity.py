@@ -104,7 +104,7 @@ def test_repeated_calls_are_stable():
 # ---- error behaviour (the reference asserts; here statuses) --------------------------------
 
 def test_self_loop_rejected():
-    g = kt.COOGraph(3, np.array([0, 1, 1, 2, 2], np.uint32), np.array([1, 0, 2, 1, 2], np.uint32))
+    g = kt.COOGraph(3, np.array([0, 1, 2, 2], np.uint32), np.array([1, 0, 2, 2], np.uint32))
     with pytest.raises(kt.KtrussError) as ei:
         kt.decompose(g)
     assert ei.value.status == 2
