@@ -152,6 +152,13 @@ __global__ void k_in_eid(const uint64_t* __restrict__ keys, uint64_t entries, un
     if (err && lane_id() == 0) atomicOr(&ctrl[kCtrlError], err);
 }
 
+// Edge id of each input entry, kept apart from s_eid because peeling compacts the rows.
+__global__ void k_entry_eid(const uint32_t* __restrict__ sorted_entry, const uint32_t* __restrict__ s_eid,
+                            uint64_t entries, uint32_t* __restrict__ entry_eid) {
+    uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < entries) entry_eid[sorted_entry[p]] = s_eid[p];
+}
+
 // First rank whose symmetric row has at least `thr` entries (rows grow with rank: ranks are
 // ascending degree), written to ctrl[kCtrlBigRow].
 __global__ void k_find_big_row(const uint32_t* __restrict__ s_ptr, uint32_t n, uint32_t thr,
@@ -247,6 +254,7 @@ int build_graph(kt_engine* e, const uint32_t* d_src, const uint32_t* d_dst, uint
     }
     const uint64_t* keys = in_b ? e->key_b : e->key_a;
     e->sorted_entry = in_b ? e->val_b : e->val_a;
+    e->entry_eid = in_b ? e->val_a : e->val_b;  // the sort's other value buffer is free now
 
     // 4. columns, split points, oriented CSR, edge ids
     k_split_init<<<grid_for(n), kThreads, 0, st>>>(e->s_ptr, n, e->s_split, e->s_len);
@@ -280,6 +288,9 @@ int build_graph(kt_engine* e, const uint32_t* d_src, const uint32_t* d_dst, uint
         k_in_eid<<<grid_for(entries), kThreads, 0, st>>>(keys, entries, vb, e->o_ptr, e->o_col, e->s_eid, e->ctrl);
         count_launch(e);
         if ((rc = check_launch(e, "k_in_eid"))) return rc;
+        k_entry_eid<<<grid_for(entries), kThreads, 0, st>>>(e->sorted_entry, e->s_eid, entries, e->entry_eid);
+        count_launch(e);
+        if ((rc = check_launch(e, "k_entry_eid"))) return rc;
     }
     k_find_big_row<<<1, 1, 0, st>>>(e->s_ptr, n, kBigRow, e->ctrl);
     count_launch(e);

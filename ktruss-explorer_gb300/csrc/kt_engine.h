@@ -36,7 +36,8 @@ struct kt_engine {
     // Per symmetric entry (2m).
     uint32_t* s_col = nullptr;    // neighbour rank
     uint32_t* s_eid = nullptr;    // edge id of the entry
-    uint32_t* sorted_entry = nullptr;  // input entry index at this sorted position
+    uint32_t* sorted_entry = nullptr;  // input entry index at this sorted position (build only)
+    uint32_t* entry_eid = nullptr;     // edge id of each input entry (outputs are gathered by it)
     // Per edge (m); edge id = position in the oriented CSR.
     uint32_t* o_col = nullptr;    // higher-rank endpoint
     uint32_t* e_src = nullptr;    // lower-rank endpoint

@@ -278,16 +278,16 @@ __global__ void k_sum_support(const uint32_t* __restrict__ sup, uint32_t m, unsi
     if (lane_id() == 0 && s) atomicAdd(total, (unsigned long long)s);
 }
 
-__global__ void k_emit_truss(const uint32_t* __restrict__ sorted_entry, const uint32_t* __restrict__ s_eid,
-                             uint64_t entries, const uint32_t* __restrict__ tr, uint32_t* __restrict__ out) {
-    uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (p < entries) out[sorted_entry[p]] = tr[s_eid[p]];
+__global__ void k_emit_truss(const uint32_t* __restrict__ entry_eid, uint64_t entries, const uint32_t* __restrict__ tr,
+                             uint32_t* __restrict__ out) {
+    uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < entries) out[i] = tr[entry_eid[i]];
 }
 
-__global__ void k_emit_keep(const uint32_t* __restrict__ sorted_entry, const uint32_t* __restrict__ s_eid,
-                            uint64_t entries, const uint32_t* __restrict__ rnd, uint8_t* __restrict__ out) {
-    uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (p < entries) out[sorted_entry[p]] = rnd[s_eid[p]] == 0 ? 1 : 0;
+__global__ void k_emit_keep(const uint32_t* __restrict__ entry_eid, uint64_t entries, const uint32_t* __restrict__ rnd,
+                            uint8_t* __restrict__ out) {
+    uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < entries) out[i] = rnd[entry_eid[i]] == 0 ? 1 : 0;
 }
 
 __global__ void k_store_u32(uint32_t* p, uint32_t v) { *p = v; }
@@ -473,8 +473,7 @@ int peel_single_k(kt_engine* e, uint32_t k) {
 int emit_truss_per_entry(kt_engine* e, uint32_t* d_out, uint32_t* d_k_max) {
     int rc;
     if (e->entries) {
-        k_emit_truss<<<grid_for(e->entries), kThreads, 0, e->stream>>>(e->sorted_entry, e->s_eid, e->entries, e->tr,
-                                                                       d_out);
+        k_emit_truss<<<grid_for(e->entries), kThreads, 0, e->stream>>>(e->entry_eid, e->entries, e->tr, d_out);
         count_launch(e);
         if ((rc = check_launch(e, "k_emit_truss"))) return rc;
     }
@@ -488,8 +487,7 @@ int emit_truss_per_entry(kt_engine* e, uint32_t* d_out, uint32_t* d_k_max) {
 
 int emit_keep(kt_engine* e, uint8_t* d_keep) {
     if (!e->entries) return KT_OK;
-    k_emit_keep<<<grid_for(e->entries), kThreads, 0, e->stream>>>(e->sorted_entry, e->s_eid, e->entries, e->rnd,
-                                                                  d_keep);
+    k_emit_keep<<<grid_for(e->entries), kThreads, 0, e->stream>>>(e->entry_eid, e->entries, e->rnd, d_keep);
     count_launch(e);
     return check_launch(e, "k_emit_keep");
 }
