@@ -189,8 +189,13 @@ int kt_engine_decompose(kt_engine* engine, const uint32_t* d_src, const uint32_t
 int kt_engine_ktruss(kt_engine* engine, const uint32_t* d_src, const uint32_t* d_dst,
                      uint64_t num_entries, uint32_t num_nodes, uint32_t k, uint8_t* d_keep,
                      int sync);
-/* Synchronizes the engine stream and fills *stats. */
+/* Synchronizes the engine stream and fills *stats.  Returns KT_ERR_TIMEOUT if the last peel
+ * kernel gave up on a grid barrier. */
 int kt_engine_stats(kt_engine* engine, kt_stats* stats);
+/* Self-test of the bounded device waits: launches a grid barrier that one block never reaches,
+ * with a wait limit of timeout_ns (at most 5 s).  Returns KT_ERR_TIMEOUT when the wait expired
+ * and the kernel returned as designed; the engine stays usable afterwards. */
+int kt_engine_selftest_barrier_timeout(kt_engine* engine, uint64_t timeout_ns);
 
 /* ---- seeded generators (no counterpart in the reference, which ships no data) --------- */
 int kt_gen_rmat(uint32_t scale, uint32_t edge_factor, double a, double b, double c,

@@ -37,7 +37,19 @@ enum : uint32_t {
     kCtrlItems0 = 12,     // work-item queue counters
     kCtrlItems1 = 13,
     kCtrlBigRow = 14,     // first rank whose symmetric row is long (block-wide compaction)
-    kCtrlWords = 16,
+    // Persistent peel kernel: barrier, outputs, and rings of per-round / per-level counters
+    // (slot r % 4 belongs to round r; slot (r+2) % 4 is cleared during round r).
+    kPBarCount = 16,
+    kPBarGen = 17,
+    kPKmax = 18,
+    kPRounds = 19,
+    kPLevels = 20,
+    kPNext = 24,       // [4] pushes into the next frontier
+    kPBigCount = 28,   // [4] long-row slots of the round
+    kPLAlive = 32,     // [4] alive edges after the level scan
+    kPLMin = 36,       // [4] minimum support over them
+    kPLFront = 40,     // [4] frontier of the level's first round
+    kCtrlWords = 48,
 };
 
 __device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }
@@ -64,5 +76,62 @@ __device__ __forceinline__ uint32_t lower_bound_u32(const uint32_t* __restrict__
 }
 
 inline uint32_t ceil_div(uint64_t a, uint64_t b) { return (uint32_t)((a + b - 1) / b); }
+
+__device__ __forceinline__ uint32_t ld_acquire(const uint32_t* p) {
+    uint32_t v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void st_release(uint32_t* p, uint32_t v) {
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+__device__ __forceinline__ uint64_t global_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Grid-wide barrier for a cooperative launch whose `expected` blocks are all resident.
+// Every wait is bounded: a block that waits longer than timeout_ns sets kErrTimeout in
+// ctrl[kCtrlError] and returns false; blocks that see the bit return false too, so the
+// kernel ends instead of hanging.  Returns true when all blocks arrived.
+__device__ __forceinline__ bool grid_barrier(uint32_t* ctrl, uint32_t expected, uint64_t timeout_ns) {
+    __shared__ uint32_t s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t ok = (ld_acquire(ctrl + kCtrlError) & kErrTimeout) ? 0u : 1u;
+        if (ok) {
+            uint32_t* gen = ctrl + kPBarGen;
+            const uint32_t g = ld_acquire(gen);
+            __threadfence();
+            if (atomicAdd(ctrl + kPBarCount, 1u) + 1 == expected) {
+                atomicExch(ctrl + kPBarCount, 0u);
+                __threadfence();
+                st_release(gen, g + 1);
+            } else {
+                const uint64_t t0 = global_ns();
+                uint32_t spins = 0, ns = 32;
+                while (ld_acquire(gen) == g) {
+                    if (ld_acquire(ctrl + kCtrlError) & kErrTimeout) { ok = 0; break; }
+                    if (global_ns() - t0 > timeout_ns) {
+                        atomicOr(ctrl + kCtrlError, kErrTimeout);
+                        ok = 0;
+                        break;
+                    }
+                    if (++spins > 64) {
+                        __nanosleep(ns);
+                        if (ns < 256) ns <<= 1;
+                    }
+                }
+            }
+            __threadfence();
+        }
+        s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
 
 }  // namespace kt

@@ -48,8 +48,7 @@ size_t carve(kt_engine* e, char* base, uint32_t n, uint64_t N) {
     const uint64_t sort_blocks = (keys + 2047) / 2048;
     const uint64_t hist_words = 256 * sort_blocks;
     const uint64_t scan_max = std::max<uint64_t>((uint64_t)n + 1, hist_words);
-    // u32 words; the u64 scan of the per-round work offsets (m+1 elements) uses it as u64
-    const uint64_t scan_words = 2 * (std::max<uint64_t>(scan_max, m + 1) / 4096 + 4096);
+    const uint64_t scan_words = scan_max / 4096 + 4096;
     Carver c{base};
     e->key_a = c.take<uint64_t>(keys);
     e->key_b = c.take<uint64_t>(keys);
@@ -72,10 +71,13 @@ size_t carve(kt_engine* e, char* base, uint32_t n, uint64_t N) {
     e->q1 = c.take<uint32_t>(m);
     e->alive0 = c.take<uint32_t>(m);
     e->alive1 = c.take<uint32_t>(m);
-    e->fx = c.take<uint32_t>(m);
     e->fy = c.take<uint32_t>(m);
     e->fbase = c.take<uint32_t>(m);
-    e->work = c.take<uint64_t>(m + 1);
+    e->flen = c.take<uint32_t>(m);
+    e->big = c.take<uint32_t>(m);
+    e->cap_rounds = (uint32_t)std::min<uint64_t>(m + 2, 1u << 22);
+    e->round_size = c.take<uint32_t>(e->cap_rounds);
+    e->round_level = c.take<uint32_t>(e->cap_rounds);
     e->hist = c.take<uint32_t>(hist_words);
     e->hist_words = hist_words;
     e->scan_tmp = c.take<uint32_t>(scan_words);
@@ -266,7 +268,10 @@ int kt_engine_decompose(kt_engine* e, const uint32_t* d_src, const uint32_t* d_d
     int rc = check_cuda(cudaSetDevice(e->device), "cudaSetDevice");
     if (rc) return rc;
     if ((rc = run_decompose(e, d_src, d_dst, num_entries, num_nodes, d_truss, d_k_max))) return rc;
-    if (sync) return check_cuda(cudaStreamSynchronize(e->stream), "synchronize");
+    if (sync) {
+        if ((rc = check_cuda(cudaStreamSynchronize(e->stream), "synchronize"))) return rc;
+        return kt::finish_stats(e);
+    }
     return KT_OK;
 }
 
@@ -278,14 +283,28 @@ int kt_engine_ktruss(kt_engine* e, const uint32_t* d_src, const uint32_t* d_dst,
     int rc = check_cuda(cudaSetDevice(e->device), "cudaSetDevice");
     if (rc) return rc;
     if ((rc = run_ktruss(e, d_src, d_dst, num_entries, num_nodes, k, d_keep))) return rc;
-    if (sync) return check_cuda(cudaStreamSynchronize(e->stream), "synchronize");
+    if (sync) {
+        if ((rc = check_cuda(cudaStreamSynchronize(e->stream), "synchronize"))) return rc;
+        return kt::finish_stats(e);
+    }
     return KT_OK;
+}
+
+int kt_engine_selftest_barrier_timeout(kt_engine* e, uint64_t timeout_ns) {
+    if (!e) return fail(KT_ERR_INVALID_ARG, "kt_engine_selftest_barrier_timeout: null engine");
+    if (timeout_ns == 0 || timeout_ns > 5000000000ull)
+        return fail(KT_ERR_INVALID_ARG, "timeout must be in (0, 5 s]");
+    int rc = check_cuda(cudaSetDevice(e->device), "cudaSetDevice");
+    if (rc) return rc;
+    e->stats_ready = true;  // the probe leaves no peel statistics behind
+    return kt::barrier_timeout_probe(e, timeout_ns);
 }
 
 int kt_engine_stats(kt_engine* e, kt_stats* stats) {
     if (!e || !stats) return fail(KT_ERR_INVALID_ARG, "kt_engine_stats: null argument");
     int rc = check_cuda(cudaStreamSynchronize(e->stream), "synchronize");
     if (rc) return rc;
+    if ((rc = kt::finish_stats(e))) return rc;
     e->stats.kernel_launches = e->launches;
     *stats = e->stats;
     return KT_OK;
@@ -313,6 +332,7 @@ int kt_decompose(const kt_coo* graph, uint32_t* truss_per_entry, uint32_t* k_max
     if (N && (rc = check_cuda(cudaMemcpyAsync(truss_per_entry, e->out_u32, N * 4, cudaMemcpyDeviceToHost, e->stream), "D2H")))
         return rc;
     if ((rc = check_cuda(cudaStreamSynchronize(e->stream), "synchronize"))) return rc;
+    if ((rc = kt::finish_stats(e))) return rc;
     if (k_max) *k_max = e->stats.k_max;
     return KT_OK;
 }
@@ -350,6 +370,7 @@ int kt_ktruss(const kt_coo* graph, kt_coo* truss, const kt_config* config) {
     for (uint32_t i = 0; i < (runs ? runs : 1); ++i) {
         if (verbose) printf("    Performing K-truss\n");
         if ((rc = run_ktruss(e, e->in_src, e->in_dst, N, graph->num_nodes, config->k, e->out_u8))) return rc;
+        if ((rc = kt::finish_stats(e))) return rc;
         if (config->verbosity == 0 && i >= config->num_warmup_runs) {
             kt_print_config_csv(config);
             printf("%f ms\n", e->stats.last_ms);

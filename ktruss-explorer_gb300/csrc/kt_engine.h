@@ -48,11 +48,11 @@ struct kt_engine {
     uint32_t* q1 = nullptr;
     uint32_t* alive0 = nullptr;   // compacted lists of alive edge ids
     uint32_t* alive1 = nullptr;
-    // Per frontier slot: shorter endpoint, other endpoint, row start, and work offsets (u64).
-    uint32_t* fx = nullptr;
+    // Per frontier slot: other endpoint, start and length of the shorter row; long-row slots.
     uint32_t* fy = nullptr;
     uint32_t* fbase = nullptr;
-    uint64_t* work = nullptr;     // m+1
+    uint32_t* flen = nullptr;
+    uint32_t* big = nullptr;
     uint32_t big_row = 0;         // ranks >= big_row have rows of kBigRow entries or more
     // Scratch for scans and sort histograms.
     uint32_t* scan_tmp = nullptr;
@@ -79,6 +79,8 @@ struct kt_engine {
     uint32_t vb = 1;  // bits per rank in sort keys
 
     kt_stats stats{};
+    int peel_mode = 0;          // 0 decomposition, 1 single-k
+    bool stats_ready = false;   // stats already read back from the device
 };
 
 namespace kt {
@@ -109,5 +111,9 @@ int peel_decompose(kt_engine* e);
 int peel_single_k(kt_engine* e, uint32_t k);
 int emit_truss_per_entry(kt_engine* e, uint32_t* d_out, uint32_t* d_k_max);
 int emit_keep(kt_engine* e, uint8_t* d_keep);
+// Reads the peel's control block and round log (stream must be drained); reports timeouts.
+int finish_stats(kt_engine* e);
+// Launches a grid barrier that cannot complete and returns the status it reports.
+int barrier_timeout_probe(kt_engine* e, uint64_t timeout_ns);
 
 }  // namespace kt

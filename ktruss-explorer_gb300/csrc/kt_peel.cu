@@ -1,24 +1,33 @@
-// Peeling: the full truss decomposition and the single-k truss.
+// Peeling: the full truss decomposition and the single-k truss, as one persistent kernel.
 //
-// Replaces the reference's host-driven count/prune loop (kernel_ddc.cu:116-214, the same
-// shape in all eight variant files) and its affected-edge recount (kernel_ddc.cu:79-114):
-// support is counted once, then kept exact by atomic decrements.
+// Replaces the reference's host-driven count/prune loop (kernel_ddc.cu:116-214, the same shape
+// in all eight variant files) and its affected-edge recount (kernel_ddc.cu:79-114): support is
+// counted once, then kept exact by atomic decrements, and the whole loop over levels and rounds
+// runs on the device in one cooperative launch (grid barriers between phases, no host round
+// trips).
 //
-// Level k removes, in synchronous rounds, the alive edges with support < k-2; each removed
-// edge gets truss number k-1.  A round's frontier is exactly the set of edges that one
-// count-and-prune pass of the reference deletes at that point, so the edge sets agree with
-// the reference pass by pass.  When an edge e = (x,y) is removed in round r, every triangle
-// (x,y,w) whose other two edges are still alive or removed in round r is destroyed once:
-// the removed edge with the smallest id among the triangle's round-r edges decrements each
-// surviving edge by one.  A decrement that takes an edge from k-2 to k-3 pushes it onto the
-// next round's frontier, so frontiers are built without scans.  A new level starts from a
-// scan of the compacted alive-edge list that also finds the minimum support, so empty levels
-// are skipped (k jumps to min+3).
+// Level k removes, in synchronous rounds, the alive edges with support < k-2; each removed edge
+// gets truss number k-1.  A round's frontier is exactly the set of edges that one count-and-prune
+// pass of the reference deletes at that point, so the edge sets agree with the reference pass by
+// pass.  When an edge e = (x,y) is removed in round r, every triangle (x,y,w) whose other two
+// edges are still alive or removed in round r is destroyed once: the removed edge with the
+// smallest id among the triangle's round-r edges decrements each surviving edge by one.  A
+// decrement that takes an edge from k-2 to k-3 pushes it onto the next round's frontier, so
+// frontiers are built without scans.  A new level starts from a warp-ballot compaction of the
+// alive-edge list that also finds the minimum support, so empty levels are skipped (k jumps to
+// min+3).
 //
-// Per-round kernels: k_mark (stamp the frontier, record each slot's work), an exclusive scan
-// of the work, k_process (find triangles, decrement, push).  Symmetric rows are compacted in
-// place once the alive edges have halved since the last compaction, so rows hold few removed
-// entries.
+// Phases of one round (grid barrier after each):
+//   mark:    stamp the frontier (round, truss number); per slot record the shorter symmetric
+//            row x, the other endpoint y, x's row start and length; long rows go to a list;
+//   process: warps walk the short rows (one slot per warp), then whole blocks walk the long
+//            rows (one slot per block); per neighbour w the edge (y,w) is found by a binary
+//            search in an oriented row.
+// Symmetric rows are compacted in place once the alive edges have halved since the last
+// compaction, so the walks see few removed entries.
+//
+// Every grid barrier wait is bounded (kPeelTimeoutNs); on expiry the kernel reports
+// KT_ERR_TIMEOUT through the control block and returns.
 
 #include <vector>
 
@@ -29,246 +38,303 @@ namespace kt {
 
 namespace {
 
-constexpr int kThreads = 256;
+constexpr int kThreads = 256;          // helper kernels
+constexpr int kPeelThreads = 1024;     // persistent kernel: one block per SM
+constexpr uint32_t kLongRow = 256;     // rows longer than this are walked by a whole block
+constexpr uint64_t kPeelTimeoutNs = 10ull * 1000 * 1000 * 1000;
 
 inline uint32_t grid_for(uint64_t n, int threads = kThreads) {
     uint64_t b = (n + threads - 1) / threads;
     return (uint32_t)(b == 0 ? 1 : b);
 }
 
-__global__ void k_init_edges(uint32_t m, uint32_t* __restrict__ rnd, uint32_t* __restrict__ tr,
-                             uint32_t* __restrict__ alive) {
-    uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j < m) {
-        rnd[j] = 0;
-        tr[j] = 0;
-        alive[j] = j;
+struct PeelParams {
+    const uint32_t* __restrict__ o_ptr;
+    const uint32_t* __restrict__ o_col;
+    const uint32_t* __restrict__ e_src;
+    const uint32_t* __restrict__ s_ptr;
+    uint32_t* s_len;
+    uint32_t* s_col;
+    uint32_t* s_eid;
+    uint32_t* sup;
+    uint32_t* rnd;
+    uint32_t* tr;
+    uint32_t* alive[2];
+    uint32_t* q[2];
+    uint32_t* fy;
+    uint32_t* fbase;
+    uint32_t* flen;
+    uint32_t* big;
+    uint32_t* ctrl;
+    uint32_t* round_size;
+    uint32_t* round_level;
+    uint32_t cap_rounds;
+    uint32_t n, m, big_row;
+    uint32_t single_k;  // 0: full decomposition; >= 3: the k of a single-k truss
+    uint64_t timeout_ns;
+};
+
+// One entry of a removed edge's shorter row: neighbour w of x at row position p.
+__device__ __forceinline__ void peel_entry(const PeelParams& P, uint32_t e, uint32_t y, uint32_t p, uint32_t r,
+                                           uint32_t km2, uint32_t* qnext, uint32_t* next_count) {
+    const uint32_t w = P.s_col[p];
+    if (w == y) return;
+    const uint32_t a = P.s_eid[p];
+    const uint32_t ra = P.rnd[a];
+    if (ra != 0 && ra != r) return;  // (x,w) removed in an earlier round: triangle already gone
+    uint32_t lo, n, target;
+    if (w > y) {
+        lo = P.o_ptr[y];
+        n = P.o_ptr[y + 1] - lo;
+        target = w;
+    } else {
+        lo = P.o_ptr[w];
+        n = P.o_ptr[w + 1] - lo;
+        target = y;
+    }
+    const uint32_t idx = lower_bound_u32(P.o_col + lo, n, target);
+    if (idx >= n || P.o_col[lo + idx] != target) return;
+    const uint32_t b = lo + idx;
+    const uint32_t rb = P.rnd[b];
+    if (rb != 0 && rb != r) return;
+    if ((ra == r && a < e) || (rb == r && b < e)) return;  // a smaller-id edge of this round owns it
+    if (ra == 0) {
+        const uint32_t old = atomicSub(&P.sup[a], 1u);
+        if (old == km2) qnext[atomicAdd(next_count, 1u)] = a;
+    }
+    if (rb == 0) {
+        const uint32_t old = atomicSub(&P.sup[b], 1u);
+        if (old == km2) qnext[atomicAdd(next_count, 1u)] = b;
     }
 }
 
-// Warp-ballot stream compaction of the alive list, with the minimum support of the survivors
-// (atomicMin into ctrl[kCtrlMin]) and the survivor count (ctrl[kCtrlCount0]).
-__global__ void k_level_scan(const uint32_t* __restrict__ alive_in, uint32_t count,
-                             const uint32_t* __restrict__ rnd, const uint32_t* __restrict__ sup,
-                             uint32_t* __restrict__ alive_out, uint32_t* __restrict__ ctrl) {
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    uint32_t e = 0, s = 0xffffffffu;
-    bool keep = false;
-    if (i < count) {
-        e = alive_in[i];
-        keep = rnd[e] == 0;
-        if (keep) s = sup[e];
-    }
-    const uint32_t ballot = __ballot_sync(kFullMask, keep);
-    uint32_t base = 0;
-    if (lane_id() == 0 && ballot) base = atomicAdd(&ctrl[kCtrlCount0], __popc(ballot));
-    base = __shfl_sync(kFullMask, base, 0);
-    if (keep) alive_out[base + __popc(ballot & lanemask_lt())] = e;
-    s = __reduce_min_sync(kFullMask, s);
-    if (lane_id() == 0 && s != 0xffffffffu) atomicMin(&ctrl[kCtrlMin], s);
-}
-
-// Frontier of a new level: alive edges with support <= thr (= k-3).
-__global__ void k_collect(const uint32_t* __restrict__ alive, uint32_t count, const uint32_t* __restrict__ sup,
-                          uint32_t thr, uint32_t* __restrict__ q, uint32_t* __restrict__ ctrl) {
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    uint32_t e = 0;
-    bool take = false;
-    if (i < count) {
-        e = alive[i];
-        take = sup[e] <= thr;
-    }
-    const uint32_t ballot = __ballot_sync(kFullMask, take);
-    uint32_t base = 0;
-    if (lane_id() == 0 && ballot) base = atomicAdd(&ctrl[kCtrlCount1], __popc(ballot));
-    base = __shfl_sync(kFullMask, base, 0);
-    if (take) q[base + __popc(ballot & lanemask_lt())] = e;
-}
-
-// Stamps the frontier edges with the round and their truss number, and records for each
-// frontier slot the shorter symmetric row (x), the other endpoint (y), x's row start and the
-// row length as the slot's work.  work[count] = 0 so that its exclusive scan ends in the total.
-__global__ void k_mark(const uint32_t* __restrict__ q, uint32_t count, uint32_t r, uint32_t truss,
-                       uint32_t* __restrict__ rnd, uint32_t* __restrict__ tr, const uint32_t* __restrict__ e_src,
-                       const uint32_t* __restrict__ o_col, const uint32_t* __restrict__ s_ptr,
-                       const uint32_t* __restrict__ s_len, uint32_t* __restrict__ fx, uint32_t* __restrict__ fy,
-                       uint32_t* __restrict__ fbase, uint64_t* __restrict__ work) {
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < count) {
-        const uint32_t e = q[i];
-        rnd[e] = r;
-        tr[e] = truss;
-        const uint32_t u = e_src[e], v = o_col[e];
-        const uint32_t lu = s_len[u], lv = s_len[v];
-        const bool ux = lu <= lv;
-        const uint32_t x = ux ? u : v;
-        fx[i] = x;
-        fy[i] = ux ? v : u;
-        fbase[i] = s_ptr[x];
-        work[i] = ux ? lu : lv;
-    } else if (i == count) {
-        work[count] = 0;
-    }
-}
-
-__global__ void k_mark_all(const uint32_t* __restrict__ q, uint32_t count, uint32_t r, uint32_t truss,
-                           uint32_t* __restrict__ rnd, uint32_t* __restrict__ tr) {
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < count) {
-        rnd[q[i]] = r;
-        tr[q[i]] = truss;
-    }
-}
-
-// Index i with offs[i] <= t < offs[i+1] in the non-decreasing offs[0, n).
-__device__ __forceinline__ uint32_t find_slot(const uint64_t* __restrict__ offs, uint32_t n, uint64_t t) {
-    uint32_t lo = 0, len = n;
-    while (len > 0) {  // upper bound of t
-        uint32_t half = len >> 1;
-        if (offs[lo + half] <= t) {
-            lo += half + 1;
-            len -= half + 1;
-        } else {
-            len = half;
-        }
-    }
-    return lo - 1;
-}
-
-constexpr int kItems = 4;  // work units per lane per warp tile
-
-// One peel round over the flattened work of the frontier: unit t belongs to the slot i with
-// offs[i] <= t < offs[i+1] and names entry t - offs[i] of that slot's shorter row.  Each warp
-// takes tiles of 32*kItems consecutive units, so long rows are spread over many warps and short
-// rows share a warp.  For a neighbour w of x (unit entry), edge (x,w) is identified by its id;
-// edge (y,w) by a binary search in an oriented row (w in N+(y) if w > y, else y in N+(w)).  The
-// triangle is skipped if either edge was removed in an earlier round or if a smaller-id edge of
-// this round owns it; otherwise each still-alive edge loses one support, and an edge whose
-// support falls from k-2 to k-3 joins the next frontier.
-__global__ void __launch_bounds__(kThreads) k_process(const uint32_t* __restrict__ q, uint32_t count,
-                                                      const uint64_t* __restrict__ offs,
-                                                      const uint32_t* __restrict__ fx,
-                                                      const uint32_t* __restrict__ fy,
-                                                      const uint32_t* __restrict__ fbase, uint32_t r, uint32_t k,
-                                                      const uint32_t* __restrict__ o_ptr,
-                                                      const uint32_t* __restrict__ o_col,
-                                                      const uint32_t* __restrict__ s_col,
-                                                      const uint32_t* __restrict__ s_eid,
-                                                      const uint32_t* __restrict__ rnd, uint32_t* __restrict__ sup,
-                                                      uint32_t* __restrict__ qnext, uint32_t* __restrict__ ctrl) {
-    const uint64_t W = offs[count];
-    const uint32_t lane = lane_id();
-    const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-    const uint32_t km2 = k - 2;
-    for (uint64_t tile = warp * (32 * kItems); tile < W; tile += nwarps * (32 * kItems)) {
-        uint64_t t = tile + lane;
-        if (t >= W) continue;
-        uint32_t i = find_slot(offs, count + 1, t);
-#pragma unroll
-        for (int s = 0; s < kItems; ++s, t += 32) {
-            if (t >= W) break;
-            while (offs[i + 1] <= t) ++i;
-            const uint32_t e = q[i], y = fy[i];
-            const uint32_t p = fbase[i] + (uint32_t)(t - offs[i]);
-            const uint32_t w = s_col[p];
-            if (w == y) continue;
-            const uint32_t a = s_eid[p];
-            const uint32_t ra = rnd[a];
-            if (ra != 0 && ra != r) continue;
-            uint32_t lo, n, target;
-            if (w > y) { lo = o_ptr[y]; n = o_ptr[y + 1] - lo; target = w; }
-            else { lo = o_ptr[w]; n = o_ptr[w + 1] - lo; target = y; }
-            const uint32_t idx = lower_bound_u32(o_col + lo, n, target);
-            if (idx >= n || o_col[lo + idx] != target) continue;
-            const uint32_t b = lo + idx;
-            const uint32_t rb = rnd[b];
-            if (rb != 0 && rb != r) continue;
-            if ((ra == r && a < e) || (rb == r && b < e)) continue;
-            if (ra == 0) {
-                uint32_t old = atomicSub(&sup[a], 1u);
-                if (old == km2) qnext[atomicAdd(&ctrl[kCtrlCount1], 1u)] = a;
-            }
-            if (rb == 0) {
-                uint32_t old = atomicSub(&sup[b], 1u);
-                if (old == km2) qnext[atomicAdd(&ctrl[kCtrlCount1], 1u)] = b;
-            }
-        }
-    }
-}
-
-// In-place ordered compaction of symmetric rows [r0, r1): entries whose edge was removed are
-// dropped, the survivors keep their order at the front of the row.  One warp per row: each
-// 32-entry step reads before any lane writes, and writes never pass the read position.
-__global__ void k_compact_rows_warp(const uint32_t* __restrict__ s_ptr, uint32_t* __restrict__ s_len,
-                                    uint32_t* __restrict__ s_col, uint32_t* __restrict__ s_eid,
-                                    const uint32_t* __restrict__ rnd, uint32_t r0, uint32_t r1) {
-    const uint32_t lane = lane_id();
+// In-place ordered compaction of the symmetric rows: warps take the short rows [0, big_row),
+// blocks the long rows [big_row, n).  Each step reads before any write of the step, and writes
+// never pass the read position.
+__device__ void compact_rows(const PeelParams& P, uint32_t* warp_cnt) {
+    const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
+    const uint32_t gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
-    for (uint32_t row = r0 + ((blockIdx.x * blockDim.x + threadIdx.x) >> 5); row < r1; row += nwarps) {
-        const uint32_t base = s_ptr[row], len = s_len[row];
+    const uint32_t big = P.big_row < P.n ? P.big_row : P.n;
+    for (uint32_t row = gwarp; row < big; row += nwarps) {
+        const uint32_t base = P.s_ptr[row], len = P.s_len[row];
         uint32_t w = 0;
         for (uint32_t i0 = 0; i0 < len; i0 += 32) {
             const uint32_t i = i0 + lane;
             uint32_t c = 0, eid = 0;
             bool keep = false;
             if (i < len) {
-                c = s_col[base + i];
-                eid = s_eid[base + i];
-                keep = rnd[eid] == 0;
+                c = P.s_col[base + i];
+                eid = P.s_eid[base + i];
+                keep = P.rnd[eid] == 0;
             }
             const uint32_t ballot = __ballot_sync(kFullMask, keep);
-            __syncwarp();  // every lane's reads of this step precede any lane's writes
+            __syncwarp();
             if (keep) {
                 const uint32_t pos = base + w + __popc(ballot & lanemask_lt());
-                s_col[pos] = c;
-                s_eid[pos] = eid;
+                P.s_col[pos] = c;
+                P.s_eid[pos] = eid;
             }
             w += __popc(ballot);
         }
-        if (lane == 0) s_len[row] = w;
+        if (lane == 0) P.s_len[row] = w;
     }
-}
-
-// The same for long rows, one block per row.
-__global__ void __launch_bounds__(kThreads) k_compact_rows_block(const uint32_t* __restrict__ s_ptr,
-                                                                 uint32_t* __restrict__ s_len,
-                                                                 uint32_t* __restrict__ s_col,
-                                                                 uint32_t* __restrict__ s_eid,
-                                                                 const uint32_t* __restrict__ rnd, uint32_t r0,
-                                                                 uint32_t r1) {
-    __shared__ uint32_t warp_cnt[kThreads / 32];
-    const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
-    for (uint32_t row = r0 + blockIdx.x; row < r1; row += gridDim.x) {
-        const uint32_t base = s_ptr[row], len = s_len[row];
+    __syncthreads();
+    for (uint32_t row = big + blockIdx.x; row < P.n; row += gridDim.x) {
+        const uint32_t base = P.s_ptr[row], len = P.s_len[row];
         uint32_t w = 0;
-        for (uint32_t i0 = 0; i0 < len; i0 += kThreads) {
+        for (uint32_t i0 = 0; i0 < len; i0 += blockDim.x) {
             const uint32_t i = i0 + threadIdx.x;
             uint32_t c = 0, eid = 0;
             bool keep = false;
             if (i < len) {
-                c = s_col[base + i];
-                eid = s_eid[base + i];
-                keep = rnd[eid] == 0;
+                c = P.s_col[base + i];
+                eid = P.s_eid[base + i];
+                keep = P.rnd[eid] == 0;
             }
             const uint32_t ballot = __ballot_sync(kFullMask, keep);
             if (lane == 0) warp_cnt[warp] = __popc(ballot);
-            __syncthreads();  // every thread has read its entry; counts are visible
+            __syncthreads();
             uint32_t before = 0, total = 0;
-            for (uint32_t x = 0; x < kThreads / 32; ++x) {
-                before += x < warp ? warp_cnt[x] : 0;
-                total += warp_cnt[x];
+            for (uint32_t x = 0; x < (blockDim.x >> 5); ++x) {
+                const uint32_t c2 = warp_cnt[x];
+                before += x < warp ? c2 : 0;
+                total += c2;
             }
             if (keep) {
                 const uint32_t pos = base + w + before + __popc(ballot & lanemask_lt());
-                s_col[pos] = c;
-                s_eid[pos] = eid;
+                P.s_col[pos] = c;
+                P.s_eid[pos] = eid;
             }
             w += total;
-            __syncthreads();  // writes of this step done before the next step's reads
+            __syncthreads();
         }
-        if (threadIdx.x == 0) s_len[row] = w;
+        if (threadIdx.x == 0) P.s_len[row] = w;
     }
+}
+
+__global__ void __launch_bounds__(kPeelThreads, 1) k_peel(PeelParams P) {
+    __shared__ uint32_t warp_cnt[kPeelThreads / 32];
+    uint32_t* ctrl = P.ctrl;
+    const uint32_t nblocks = gridDim.x;
+    const uint32_t lane = lane_id();
+    const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const uint64_t nthreads = (uint64_t)gridDim.x * blockDim.x;
+    const uint32_t gwarp = (uint32_t)(tid >> 5);
+    const uint32_t nwarps = (uint32_t)(nthreads >> 5);
+    const bool leader = blockIdx.x == 0 && threadIdx.x == 0;
+
+    for (uint64_t j = tid; j < P.m; j += nthreads) {
+        P.rnd[j] = 0;
+        P.tr[j] = 0;
+        P.alive[0][j] = (uint32_t)j;
+    }
+    if (!grid_barrier(ctrl, nblocks, P.timeout_ns)) return;
+
+    uint32_t cur = 0, qc = 0, count = P.m, r = 0, level = 0, k = 3, k_last = 2;
+    uint64_t live = P.m, live_at_compaction = P.m;
+    for (;;) {
+        const uint32_t ls = level & 3;
+        if (P.single_k == 0) {
+            // level scan: compact the alive list, minimum support of the survivors
+            if (leader) {
+                const uint32_t z = (level + 2) & 3;
+                ctrl[kPLAlive + z] = 0;
+                ctrl[kPLMin + z] = 0xffffffffu;
+                ctrl[kPLFront + z] = 0;
+            }
+            const uint32_t* ain = P.alive[cur];
+            uint32_t* aout = P.alive[cur ^ 1];
+            for (uint64_t i0 = (uint64_t)gwarp * 32; i0 < count; i0 += (uint64_t)nwarps * 32) {
+                const uint64_t i = i0 + lane;
+                uint32_t e = 0, s = 0xffffffffu;
+                bool keep = false;
+                if (i < count) {
+                    e = ain[i];
+                    keep = P.rnd[e] == 0;
+                    if (keep) s = P.sup[e];
+                }
+                const uint32_t ballot = __ballot_sync(kFullMask, keep);
+                uint32_t base = 0;
+                if (lane == 0 && ballot) base = atomicAdd(ctrl + kPLAlive + ls, __popc(ballot));
+                base = __shfl_sync(kFullMask, base, 0);
+                if (keep) aout[base + __popc(ballot & lanemask_lt())] = e;
+                s = __reduce_min_sync(kFullMask, s);
+                if (lane == 0 && s != 0xffffffffu) atomicMin(ctrl + kPLMin + ls, s);
+            }
+            if (!grid_barrier(ctrl, nblocks, P.timeout_ns)) return;
+            count = ld_acquire(ctrl + kPLAlive + ls);
+            if (count == 0) break;
+            k = ld_acquire(ctrl + kPLMin + ls) + 3;
+            cur ^= 1;
+        } else {
+            k = P.single_k;
+            if (leader) ctrl[kPLFront + ls] = 0;
+            if (!grid_barrier(ctrl, nblocks, P.timeout_ns)) return;
+        }
+        // frontier of the level's first round: alive edges with support <= k-3
+        {
+            const uint32_t* al = P.alive[cur];
+            uint32_t* q = P.q[qc];
+            const uint32_t thr = k - 3;
+            for (uint64_t i0 = (uint64_t)gwarp * 32; i0 < count; i0 += (uint64_t)nwarps * 32) {
+                const uint64_t i = i0 + lane;
+                uint32_t e = 0;
+                bool take = false;
+                if (i < count) {
+                    e = al[i];
+                    take = P.sup[e] <= thr;
+                }
+                const uint32_t ballot = __ballot_sync(kFullMask, take);
+                uint32_t base = 0;
+                if (lane == 0 && ballot) base = atomicAdd(ctrl + kPLFront + ls, __popc(ballot));
+                base = __shfl_sync(kFullMask, base, 0);
+                if (take) q[base + __popc(ballot & lanemask_lt())] = e;
+            }
+        }
+        if (!grid_barrier(ctrl, nblocks, P.timeout_ns)) return;
+        uint32_t F = ld_acquire(ctrl + kPLFront + ls);
+        const uint32_t km2 = k - 2;
+        while (F) {
+            if (live * 2 < live_at_compaction) {
+                compact_rows(P, warp_cnt);
+                if (!grid_barrier(ctrl, nblocks, P.timeout_ns)) return;
+                live_at_compaction = live;
+            }
+            ++r;
+            const uint32_t rs = r & 3;
+            // mark
+            if (leader) {
+                const uint32_t z = (r + 2) & 3;
+                ctrl[kPNext + z] = 0;
+                ctrl[kPBigCount + z] = 0;
+                if (r < P.cap_rounds) {
+                    P.round_size[r] = F;
+                    P.round_level[r] = k;
+                }
+            }
+            {
+                const uint32_t* q = P.q[qc];
+                for (uint64_t i = tid; i < F; i += nthreads) {
+                    const uint32_t e = q[i];
+                    P.rnd[e] = r;
+                    P.tr[e] = k - 1;
+                    const uint32_t u = P.e_src[e], v = P.o_col[e];
+                    const uint32_t lu = P.s_len[u], lv = P.s_len[v];
+                    const bool ux = lu <= lv;
+                    const uint32_t x = ux ? u : v, len = ux ? lu : lv;
+                    P.fy[i] = ux ? v : u;
+                    P.fbase[i] = P.s_ptr[x];
+                    P.flen[i] = len;
+                    if (len > kLongRow) P.big[atomicAdd(ctrl + kPBigCount + rs, 1u)] = (uint32_t)i;
+                }
+            }
+            if (!grid_barrier(ctrl, nblocks, P.timeout_ns)) return;
+            // process
+            {
+                const uint32_t* q = P.q[qc];
+                uint32_t* qnext = P.q[qc ^ 1];
+                uint32_t* next_count = ctrl + kPNext + rs;
+                for (uint32_t i = gwarp; i < F; i += nwarps) {
+                    const uint32_t len = P.flen[i];
+                    if (len > kLongRow) continue;
+                    const uint32_t e = q[i], y = P.fy[i], base = P.fbase[i];
+                    for (uint32_t t = lane; t < len; t += 32) peel_entry(P, e, y, base + t, r, km2, qnext, next_count);
+                }
+                __syncthreads();
+                const uint32_t nbig = ld_acquire(ctrl + kPBigCount + rs);
+                for (uint32_t j = blockIdx.x; j < nbig; j += nblocks) {
+                    const uint32_t i = P.big[j];
+                    const uint32_t e = q[i], y = P.fy[i], base = P.fbase[i], len = P.flen[i];
+                    for (uint32_t t = threadIdx.x; t < len; t += blockDim.x)
+                        peel_entry(P, e, y, base + t, r, km2, qnext, next_count);
+                }
+            }
+            if (!grid_barrier(ctrl, nblocks, P.timeout_ns)) return;
+            live -= F;
+            F = ld_acquire(ctrl + kPNext + rs);
+            qc ^= 1;
+        }
+        ++level;
+        k_last = k;
+        if (P.single_k != 0) break;
+    }
+    if (leader) {
+        ctrl[kPKmax] = P.single_k ? 0 : k_last - 1;
+        ctrl[kPRounds] = r;
+        ctrl[kPLevels] = level;
+    }
+}
+
+// A barrier that cannot complete (it expects one block more than the grid has): every wait
+// runs out after timeout_ns and the kernel returns with kErrTimeout set.
+__global__ void k_barrier_probe(uint32_t* ctrl, uint64_t timeout_ns) {
+    grid_barrier(ctrl, gridDim.x + 1, timeout_ns);
+}
+
+__global__ void k_init_peel_ctrl(uint32_t* ctrl) {
+    const uint32_t i = threadIdx.x;
+    if (i >= kPBarCount && i < kCtrlWords) ctrl[i] = (i >= kPLMin && i < kPLMin + 4) ? 0xffffffffu : 0u;
 }
 
 __global__ void k_sum_support(const uint32_t* __restrict__ sup, uint32_t m, unsigned long long* __restrict__ total) {
@@ -290,76 +356,57 @@ __global__ void k_emit_keep(const uint32_t* __restrict__ entry_eid, uint64_t ent
     if (i < entries) out[i] = rnd[entry_eid[i]] == 0 ? 1 : 0;
 }
 
-__global__ void k_store_u32(uint32_t* p, uint32_t v) { *p = v; }
+__global__ void k_copy_u32(uint32_t* dst, const uint32_t* src) { *dst = *src; }
 
-int read_ctrl(kt_engine* e) {
-    int rc = check_cuda(cudaMemcpyAsync(e->h_ctrl, e->ctrl, sizeof(uint32_t) * kCtrlWords, cudaMemcpyDeviceToHost,
-                                        e->stream), "read control block");
-    if (rc) return rc;
-    return check_cuda(cudaStreamSynchronize(e->stream), "peel synchronize");
+__global__ void k_fill_edges(uint32_t m, uint32_t value, uint32_t* __restrict__ rnd) {
+    uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < m) rnd[j] = value;
 }
 
-int set_ctrl(kt_engine* e, uint32_t word, uint32_t value) {
-    k_store_u32<<<1, 1, 0, e->stream>>>(e->ctrl + word, value);
+int launch_peel(kt_engine* e, uint32_t single_k) {
+    int rc;
+    k_init_peel_ctrl<<<1, kCtrlWords, 0, e->stream>>>(e->ctrl);
     count_launch(e);
-    return check_launch(e, "k_store_u32");
-}
-
-// Drops removed edges from every symmetric row.
-int compact_rows(kt_engine* e) {
-    int rc;
-    const uint32_t big = e->big_row < e->n ? e->big_row : e->n;
-    if (big > 0) {
-        uint64_t blocks = ((uint64_t)big * 32 + kThreads - 1) / kThreads;
-        uint64_t cap = (uint64_t)e->num_sms * 8;
-        k_compact_rows_warp<<<(uint32_t)(blocks < cap ? blocks : cap), kThreads, 0, e->stream>>>(
-            e->s_ptr, e->s_len, e->s_col, e->s_eid, e->rnd, 0, big);
-        count_launch(e);
-        if ((rc = check_launch(e, "k_compact_rows_warp"))) return rc;
-    }
-    if (big < e->n) {
-        uint32_t rows = e->n - big;
-        uint32_t blocks = rows < (uint32_t)e->num_sms * 4 ? rows : (uint32_t)e->num_sms * 4;
-        k_compact_rows_block<<<blocks, kThreads, 0, e->stream>>>(e->s_ptr, e->s_len, e->s_col, e->s_eid, e->rnd, big,
-                                                                 e->n);
-        count_launch(e);
-        if ((rc = check_launch(e, "k_compact_rows_block"))) return rc;
-    }
-    return KT_OK;
-}
-
-// Runs rounds at level k from the frontier in q0 (count F) until no edge falls below k-2.
-// Appends each round's frontier size to `sizes`.  Rows are compacted between rounds once the
-// alive edges have halved since the last compaction.
-int run_rounds(kt_engine* e, uint32_t k, uint32_t F, uint32_t* r, std::vector<uint32_t>& sizes, uint64_t* alive,
-               uint64_t* alive_at_compaction) {
-    int rc;
-    const uint32_t process_blocks = (uint32_t)e->num_sms * 8;
-    while (F) {
-        if (*alive * 2 < *alive_at_compaction) {
-            if ((rc = compact_rows(e))) return rc;
-            *alive_at_compaction = *alive;
-        }
-        ++*r;
-        sizes.push_back(F);
-        k_mark<<<grid_for((uint64_t)F + 1), kThreads, 0, e->stream>>>(e->q0, F, *r, k - 1, e->rnd, e->tr, e->e_src,
-                                                                      e->o_col, e->s_ptr, e->s_len, e->fx, e->fy,
-                                                                      e->fbase, e->work);
-        count_launch(e);
-        if ((rc = check_launch(e, "k_mark"))) return rc;
-        if ((rc = exclusive_scan_u64(e, e->work, e->work, (uint64_t)F + 1))) return rc;
-        if ((rc = set_ctrl(e, kCtrlCount1, 0))) return rc;
-        k_process<<<process_blocks, kThreads, 0, e->stream>>>(e->q0, F, e->work, e->fx, e->fy, e->fbase, *r, k,
-                                                              e->o_ptr, e->o_col, e->s_col, e->s_eid, e->rnd, e->sup,
-                                                              e->q1, e->ctrl);
-        count_launch(e);
-        if ((rc = check_launch(e, "k_process"))) return rc;
-        if ((rc = read_ctrl(e))) return rc;
-        *alive -= F;
-        F = e->h_ctrl[kCtrlCount1];
-        std::swap(e->q0, e->q1);
-    }
-    return KT_OK;
+    if ((rc = check_launch(e, "k_init_peel_ctrl"))) return rc;
+    int per_sm = 0;
+    if ((rc = check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_peel, kPeelThreads, 0),
+                         "occupancy of k_peel")))
+        return rc;
+    if (per_sm < 1) return fail(KT_ERR_CUDA, "k_peel cannot be resident (occupancy 0)");
+    PeelParams P;
+    P.o_ptr = e->o_ptr;
+    P.o_col = e->o_col;
+    P.e_src = e->e_src;
+    P.s_ptr = e->s_ptr;
+    P.s_len = e->s_len;
+    P.s_col = e->s_col;
+    P.s_eid = e->s_eid;
+    P.sup = e->sup;
+    P.rnd = e->rnd;
+    P.tr = e->tr;
+    P.alive[0] = e->alive0;
+    P.alive[1] = e->alive1;
+    P.q[0] = e->q0;
+    P.q[1] = e->q1;
+    P.fy = e->fy;
+    P.fbase = e->fbase;
+    P.flen = e->flen;
+    P.big = e->big;
+    P.ctrl = e->ctrl;
+    P.round_size = e->round_size;
+    P.round_level = e->round_level;
+    P.cap_rounds = e->cap_rounds;
+    P.n = e->n;
+    P.m = e->m;
+    P.big_row = e->big_row;
+    P.single_k = single_k;
+    P.timeout_ns = kPeelTimeoutNs;
+    void* args[] = {&P};
+    rc = check_cuda(cudaLaunchCooperativeKernel((const void*)k_peel, dim3((unsigned)e->num_sms), dim3(kPeelThreads),
+                                                args, 0, e->stream),
+                    "cooperative launch of k_peel");
+    count_launch(e);
+    return rc;
 }
 
 int triangles(kt_engine* e) {
@@ -377,97 +424,29 @@ int triangles(kt_engine* e) {
 }  // namespace
 
 int peel_decompose(kt_engine* e) {
-    const uint32_t m = e->m;
     int rc;
-    e->stats.k_max = 0;
-    e->stats.num_levels = 0;
-    e->stats.num_rounds = 0;
-    e->stats.plain_passes = 0;
-    e->stats.plain_alive_sum = 0;
+    e->peel_mode = 0;
+    e->stats_ready = false;
     if ((rc = triangles(e))) return rc;
-    if (m == 0) return KT_OK;
-    k_init_edges<<<grid_for(m), kThreads, 0, e->stream>>>(m, e->rnd, e->tr, e->alive0);
-    count_launch(e);
-    if ((rc = check_launch(e, "k_init_edges"))) return rc;
-    if ((rc = read_ctrl(e))) return rc;
-    e->stats.triangles = ((uint64_t)e->h_ctrl[kCtrlTriHi] << 32 | e->h_ctrl[kCtrlTriLo]) / 3;
-
-    // pass statistics of the reference chain (level 3 is one pass over all m edges, each
-    // level k >= 4 up to k_max+1 one pass per removing round plus a final one)
-    uint64_t alive = m, passes = 1, alive_sum = m;
-    uint64_t live = m, live_at_compaction = m;
-    uint32_t count = m, r = 0, k = 3, k_last = 2;
-    std::vector<uint32_t> sizes;
-    for (;;) {
-        if ((rc = set_ctrl(e, kCtrlCount0, 0))) return rc;
-        if ((rc = set_ctrl(e, kCtrlMin, 0xffffffffu))) return rc;
-        k_level_scan<<<grid_for(count), kThreads, 0, e->stream>>>(e->alive0, count, e->rnd, e->sup, e->alive1, e->ctrl);
-        count_launch(e);
-        if ((rc = check_launch(e, "k_level_scan"))) return rc;
-        if ((rc = read_ctrl(e))) return rc;
-        count = e->h_ctrl[kCtrlCount0];
-        std::swap(e->alive0, e->alive1);
-        if (count == 0) break;
-        const uint32_t mn = e->h_ctrl[kCtrlMin];
-        const uint32_t next_k = mn + 3;
-        for (uint32_t kk = k > 3 ? k : 4; kk < next_k; ++kk) { passes++; alive_sum += alive; }
-        k = next_k;
-        if ((rc = set_ctrl(e, kCtrlCount1, 0))) return rc;
-        k_collect<<<grid_for(count), kThreads, 0, e->stream>>>(e->alive0, count, e->sup, k - 3, e->q0, e->ctrl);
-        count_launch(e);
-        if ((rc = check_launch(e, "k_collect"))) return rc;
-        if ((rc = read_ctrl(e))) return rc;
-        const uint32_t F = e->h_ctrl[kCtrlCount1];
-        sizes.clear();
-        if ((rc = run_rounds(e, k, F, &r, sizes, &live, &live_at_compaction))) return rc;
-        for (uint32_t s : sizes) {
-            if (k >= 4) { passes++; alive_sum += alive; }
-            alive -= s;
-        }
-        if (k >= 4) { passes++; alive_sum += alive; }
-        e->stats.num_levels++;
-        k_last = k;
-        ++k;
-    }
-    e->stats.k_max = k_last - 1;
-    e->stats.num_rounds = r;
-    e->stats.plain_passes = (uint32_t)passes;
-    e->stats.plain_alive_sum = alive_sum;
-    return KT_OK;
+    if (e->m == 0) return KT_OK;
+    return launch_peel(e, 0);
 }
 
 int peel_single_k(kt_engine* e, uint32_t k) {
-    const uint32_t m = e->m;
     int rc;
-    e->stats.num_rounds = 0;
-    e->stats.triangles = 0;
+    e->peel_mode = 1;
+    e->stats_ready = false;
     if (k >= 3 && (rc = triangles(e))) return rc;
-    if (m == 0) return KT_OK;
-    k_init_edges<<<grid_for(m), kThreads, 0, e->stream>>>(m, e->rnd, e->tr, e->alive0);
-    count_launch(e);
-    if ((rc = check_launch(e, "k_init_edges"))) return rc;
+    if (e->m == 0) return KT_OK;
     if (k < 3) {
         // k = 2 keeps every edge; k < 2 removes every edge (k-2 wraps as unsigned, as in
         // mark_deleted_edges_kernel, kernel_ddc.cu:64)
-        if (k < 2) {
-            k_mark_all<<<grid_for(m), kThreads, 0, e->stream>>>(e->alive0, m, 1, 1, e->rnd, e->tr);
-            count_launch(e);
-            if ((rc = check_launch(e, "k_mark_all"))) return rc;
-        }
-        return KT_OK;
+        e->peel_mode = 2;
+        k_fill_edges<<<grid_for(e->m), kThreads, 0, e->stream>>>(e->m, k < 2 ? 1u : 0u, e->rnd);
+        count_launch(e);
+        return check_launch(e, "k_fill_edges");
     }
-    if ((rc = set_ctrl(e, kCtrlCount1, 0))) return rc;
-    k_collect<<<grid_for(m), kThreads, 0, e->stream>>>(e->alive0, m, e->sup, k - 3, e->q0, e->ctrl);
-    count_launch(e);
-    if ((rc = check_launch(e, "k_collect"))) return rc;
-    if ((rc = read_ctrl(e))) return rc;
-    e->stats.triangles = ((uint64_t)e->h_ctrl[kCtrlTriHi] << 32 | e->h_ctrl[kCtrlTriLo]) / 3;
-    uint32_t r = 0;
-    uint64_t live = m, live_at_compaction = m;
-    std::vector<uint32_t> sizes;
-    if ((rc = run_rounds(e, k, e->h_ctrl[kCtrlCount1], &r, sizes, &live, &live_at_compaction))) return rc;
-    e->stats.num_rounds = r;
-    return KT_OK;
+    return launch_peel(e, k);
 }
 
 int emit_truss_per_entry(kt_engine* e, uint32_t* d_out, uint32_t* d_k_max) {
@@ -478,9 +457,13 @@ int emit_truss_per_entry(kt_engine* e, uint32_t* d_out, uint32_t* d_k_max) {
         if ((rc = check_launch(e, "k_emit_truss"))) return rc;
     }
     if (d_k_max) {
-        k_store_u32<<<1, 1, 0, e->stream>>>(d_k_max, e->stats.k_max);
+        if (e->m) {
+            k_copy_u32<<<1, 1, 0, e->stream>>>(d_k_max, e->ctrl + kPKmax);
+        } else {
+            if ((rc = check_cuda(cudaMemsetAsync(d_k_max, 0, sizeof(uint32_t), e->stream), "clear k_max"))) return rc;
+        }
         count_launch(e);
-        if ((rc = check_launch(e, "k_store_u32"))) return rc;
+        if ((rc = check_launch(e, "k_copy_u32"))) return rc;
     }
     return KT_OK;
 }
@@ -490,6 +473,78 @@ int emit_keep(kt_engine* e, uint8_t* d_keep) {
     k_emit_keep<<<grid_for(e->entries), kThreads, 0, e->stream>>>(e->entry_eid, e->entries, e->rnd, d_keep);
     count_launch(e);
     return check_launch(e, "k_emit_keep");
+}
+
+// Reads the control block and the round log after the stream has drained; fills the peel
+// statistics, including the pass statistics of the reference's chained schedule: level 3 is
+// one pass over all m edges; each level k >= 4 up to k_max+1 takes one pass per removing round
+// plus a final pass, each seeing the edges alive at its start; levels that remove nothing take
+// one pass each.
+int finish_stats(kt_engine* e) {
+    if (e->stats_ready) return KT_OK;
+    if (e->m == 0 || e->peel_mode == 2) {
+        e->stats.k_max = 0;
+        e->stats.num_rounds = e->stats.num_levels = e->stats.plain_passes = 0;
+        e->stats.plain_alive_sum = 0;
+        e->stats.triangles = 0;
+        e->stats_ready = true;
+        return KT_OK;
+    }
+    int rc = check_cuda(cudaMemcpy(e->h_ctrl, e->ctrl, sizeof(uint32_t) * kCtrlWords, cudaMemcpyDeviceToHost),
+                        "read control block");
+    if (rc) return rc;
+    const uint32_t err = e->h_ctrl[kCtrlError];
+    if (err & kErrTimeout) return fail(KT_ERR_TIMEOUT, "a grid barrier wait of the peel kernel expired");
+    const uint64_t m = e->m;
+    e->stats.triangles = ((uint64_t)e->h_ctrl[kCtrlTriHi] << 32 | e->h_ctrl[kCtrlTriLo]) / 3;
+    e->stats.k_max = m ? (e->peel_mode == 0 ? e->h_ctrl[kPKmax] : 0) : 0;
+    e->stats.num_rounds = m ? e->h_ctrl[kPRounds] : 0;
+    e->stats.num_levels = m ? e->h_ctrl[kPLevels] : 0;
+    e->stats.plain_passes = 0;
+    e->stats.plain_alive_sum = 0;
+    const uint32_t R = e->stats.num_rounds;
+    if (e->peel_mode == 0 && m && R < e->cap_rounds) {
+        std::vector<uint32_t> size(R + 1), lvl(R + 1);
+        if (R && ((rc = check_cuda(cudaMemcpy(size.data(), e->round_size, sizeof(uint32_t) * (R + 1),
+                                              cudaMemcpyDeviceToHost), "read round log")) ||
+                  (rc = check_cuda(cudaMemcpy(lvl.data(), e->round_level, sizeof(uint32_t) * (R + 1),
+                                              cudaMemcpyDeviceToHost), "read round log"))))
+            return rc;
+        uint64_t alive = m, passes = 1, alive_sum = m;
+        uint32_t next_k = 3;
+        for (uint32_t r = 1; r <= R;) {
+            const uint32_t k = lvl[r];
+            for (uint32_t kk = next_k > 4 ? next_k : 4; kk < k; ++kk) { passes++; alive_sum += alive; }
+            while (r <= R && lvl[r] == k) {
+                if (k >= 4) { passes++; alive_sum += alive; }
+                alive -= size[r];
+                ++r;
+            }
+            if (k >= 4) { passes++; alive_sum += alive; }
+            next_k = k + 1;
+        }
+        e->stats.plain_passes = (uint32_t)passes;
+        e->stats.plain_alive_sum = alive_sum;
+    }
+    e->stats_ready = true;
+    return KT_OK;
+}
+
+int barrier_timeout_probe(kt_engine* e, uint64_t timeout_ns) {
+    int rc = check_cuda(cudaMemsetAsync(e->ctrl, 0, sizeof(uint32_t) * kCtrlWords, e->stream), "clear control block");
+    if (rc) return rc;
+    uint32_t* ctrl = e->ctrl;
+    void* args[] = {&ctrl, &timeout_ns};
+    if ((rc = check_cuda(cudaLaunchCooperativeKernel((const void*)k_barrier_probe, dim3(2), dim3(32), args, 0, e->stream),
+                         "cooperative launch of k_barrier_probe")))
+        return rc;
+    count_launch(e);
+    if ((rc = check_cuda(cudaStreamSynchronize(e->stream), "synchronize"))) return rc;
+    if ((rc = check_cuda(cudaMemcpy(e->h_ctrl, e->ctrl, sizeof(uint32_t) * kCtrlWords, cudaMemcpyDeviceToHost),
+                         "read control block")))
+        return rc;
+    if (e->h_ctrl[kCtrlError] & kErrTimeout) return fail(KT_ERR_TIMEOUT, "barrier probe: wait expired as intended");
+    return KT_OK;
 }
 
 }  // namespace kt

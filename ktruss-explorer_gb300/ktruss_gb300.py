@@ -108,6 +108,7 @@ def lib() -> ctypes.CDLL:
         L.kt_engine_ktruss.argtypes = [_VP, _VP, _VP, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32, _VP,
                                        ctypes.c_int]
         L.kt_engine_stats.argtypes = [_VP, ctypes.POINTER(Stats)]
+        L.kt_engine_selftest_barrier_timeout.argtypes = [_VP, ctypes.c_uint64]
         for g in ("kt_gen_rmat",):
             getattr(L, g).argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_double, ctypes.c_double,
                                       ctypes.c_double, ctypes.c_uint64, ctypes.POINTER(_Edges)]
@@ -317,6 +318,10 @@ class Engine:
                sync: bool = True) -> None:
         _check(lib().kt_engine_ktruss(self._h, d_src, d_dst, num_entries, num_nodes, k & 0xFFFFFFFF, d_keep,
                                       int(sync)))
+
+    def selftest_barrier_timeout(self, timeout_ns: int) -> int:
+        """Status of a grid barrier that cannot complete (KT_ERR_TIMEOUT = 11 when correct)."""
+        return lib().kt_engine_selftest_barrier_timeout(self._h, timeout_ns)
 
     def stats(self) -> Stats:
         s = Stats()

@@ -156,3 +156,37 @@ def test_engine_after_error_still_usable():
     n, u, v, t = load_golden("k6")
     truss, k_max = kt.decompose(kt.COOGraph.from_undirected(n, u, v))
     assert k_max == 6
+
+
+def test_barrier_wait_is_bounded_and_engine_recovers():
+    """A grid barrier that one block never reaches gives up after its limit and reports
+    KT_ERR_TIMEOUT; the context stays usable (failure detection without a GPU fault)."""
+    eng = kt.Engine(0)
+    assert eng.selftest_barrier_timeout(50_000_000) == 11  # KT_ERR_TIMEOUT after 50 ms
+    n, u, v, t = load_golden("tiny9")
+    src, dst = both_directions(u, v)
+    import torch
+    d_src = torch.from_numpy(src.view(np.int32)).cuda()
+    d_dst = torch.from_numpy(dst.view(np.int32)).cuda()
+    d_out = torch.zeros(len(src), dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    eng.decompose(d_src.data_ptr(), d_dst.data_ptr(), len(src), n, d_out.data_ptr())
+    assert np.array_equal(d_out.cpu().numpy().view(np.uint32)[: len(u)], t)
+    eng.close()
+
+
+@pytest.mark.parametrize("k", [2, 3, 5, 9])
+def test_engine_single_k_keep_mask(k):
+    torch = pytest.importorskip("torch")
+    n, u, v = kt.gen_rmat(13, 16, 0.57, 0.19, 0.19, 7)
+    src, dst = both_directions(u, v)
+    eng = kt.Engine(0)
+    d_src = torch.from_numpy(src.view(np.int32)).cuda()
+    d_dst = torch.from_numpy(dst.view(np.int32)).cuda()
+    d_keep = torch.zeros(len(src), dtype=torch.uint8, device="cuda")
+    torch.cuda.synchronize()
+    eng.ktruss(d_src.data_ptr(), d_dst.data_ptr(), len(src), n, k, d_keep.data_ptr())
+    keep = d_keep.cpu().numpy().astype(bool)
+    os_, od = oracle.ktruss(n, src, dst, k)
+    assert np.array_equal(edge_keys(src[keep], dst[keep]), edge_keys(os_, od))
+    eng.close()
