@@ -281,7 +281,8 @@ def run_ours(args, world, rank, local):
                        "triangles": st.triangles, "peel_rounds": st.num_rounds, "peel_levels": st.num_levels,
                        "parallelism": f"replicas{world}", "l2": "input entries 2x4x2m bytes > L2 (129 MB)",
                        "phase_ms": {"build": statistics.mean(build_ms), "support": sup_ms,
-                                    "peel": statistics.mean(peel_ms)}},
+                                    "peel": statistics.mean(peel_ms)},
+                       "peel_phase_ms": st.as_dict()["peel_phase_ms"], "compactions": st.compactions},
             "e2e": {"value": m * world / e2e_s, "unit": "edges/s", "h2d_bytes_per_step": 8 * N,
                     "d2h_bytes_per_step": 4 * N},
             "gpu_launches": launches // args.steps * args.steps,

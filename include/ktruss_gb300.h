@@ -168,6 +168,10 @@ typedef struct kt_stats {
     float build_ms;              /* of which: device CSR build (relabel, sort, orient)        */
     float support_ms;            /*           support count                                   */
     float peel_ms;               /*           peeling and output                              */
+    uint32_t compactions;        /* in-place compactions of the adjacency rows while peeling   */
+    float peel_phase_ms[6];      /* peel kernel time by phase (init, level scan, frontier
+                                    collection, row compaction, mark, process), barrier to
+                                    barrier, as seen by its first block                        */
 } kt_stats;
 
 /* Creates an engine on `device` with its own non-blocking CUDA stream. */

@@ -49,7 +49,10 @@ enum : uint32_t {
     kPLAlive = 32,     // [4] alive edges after the level scan
     kPLMin = 36,       // [4] minimum support over them
     kPLFront = 40,     // [4] frontier of the level's first round
-    kCtrlWords = 48,
+    kPCompactions = 44,
+    kPPhaseNs = 48,    // [6] u64 nanoseconds per phase kind (init, level scan, collect,
+                       //     compaction, mark, process), measured by block 0 barrier to barrier
+    kCtrlWords = 64,
 };
 
 __device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }

@@ -17,12 +17,15 @@
 // alive-edge list that also finds the minimum support, so empty levels are skipped (k jumps to
 // min+3).
 //
-// Phases of one round (grid barrier after each):
-//   mark:    stamp the frontier (round, truss number); per slot record the shorter symmetric
-//            row x, the other endpoint y, x's row start and length; long rows go to a list;
-//   process: warps walk the short rows (one slot per warp), then whole blocks walk the long
-//            rows (one slot per block); per neighbour w the edge (y,w) is found by a binary
-//            search in an oriented row.
+// One round is one phase followed by one grid barrier: warps walk the frontier edges' short
+// rows (one edge per warp, or several warps per edge when the frontier is small), then whole
+// blocks walk the long rows; per neighbour w of the shorter row's vertex x, the edge (y,w) is
+// found by a binary search in an oriented row.  An edge is stamped with the next round number
+// when its support falls below the threshold, and filed in the next round's short- or
+// long-row queue, so no separate marking phase is needed.  A removed edge's support is set to
+// kDead, so a level's scan of the alive list reads one array; that scan also collects the
+// frontier of level k_last+1, and only when that level turns out to be empty does a second
+// pass collect the frontier of the next non-empty level.
 // Symmetric rows are compacted in place once the alive edges have halved since the last
 // compaction, so the walks see few removed entries.
 //
@@ -60,11 +63,8 @@ struct PeelParams {
     uint32_t* rnd;
     uint32_t* tr;
     uint32_t* alive[2];
-    uint32_t* q[2];
-    uint32_t* fy;
-    uint32_t* fbase;
-    uint32_t* flen;
-    uint32_t* big;
+    uint32_t* q[2];    // frontier slots with short rows, by round parity
+    uint32_t* big[2];  // frontier slots with long rows, by round parity
     uint32_t* ctrl;
     uint32_t* round_size;
     uint32_t* round_level;
@@ -74,14 +74,29 @@ struct PeelParams {
     uint64_t timeout_ns;
 };
 
-// One entry of a removed edge's shorter row: neighbour w of x at row position p.
+constexpr uint32_t kDead = 0xffffffffu;  // support of a removed edge
+
+// Queues an edge for round rr: stamps it and files it by the length of its shorter row
+// (a scheduling hint; the row is measured again when the round runs).
+__device__ __forceinline__ void push_edge(const PeelParams& P, uint32_t e, uint32_t rr) {
+    P.rnd[e] = rr;
+    const uint32_t lu = P.s_len[P.e_src[e]], lv = P.s_len[P.o_col[e]];
+    const uint32_t len = lu < lv ? lu : lv;
+    const uint32_t slot = rr & 3;
+    if (len > kLongRow) P.big[rr & 1][atomicAdd(P.ctrl + kPBigCount + slot, 1u)] = e;
+    else P.q[rr & 1][atomicAdd(P.ctrl + kPNext + slot, 1u)] = e;
+}
+
+// One entry of a removed edge's shorter row: neighbour w of x at row position p.  Edge states
+// during round r: rnd 0 = alive, r+1 = alive but queued for the next round, r = removed in this
+// round, 1..r-1 = removed earlier.
 __device__ __forceinline__ void peel_entry(const PeelParams& P, uint32_t e, uint32_t y, uint32_t p, uint32_t r,
-                                           uint32_t km2, uint32_t* qnext, uint32_t* next_count) {
+                                           uint32_t km2) {
     const uint32_t w = P.s_col[p];
     if (w == y) return;
     const uint32_t a = P.s_eid[p];
     const uint32_t ra = P.rnd[a];
-    if (ra != 0 && ra != r) return;  // (x,w) removed in an earlier round: triangle already gone
+    if (ra != 0 && ra < r) return;  // (x,w) removed in an earlier round: triangle already gone
     uint32_t lo, n, target;
     if (w > y) {
         lo = P.o_ptr[y];
@@ -96,22 +111,33 @@ __device__ __forceinline__ void peel_entry(const PeelParams& P, uint32_t e, uint
     if (idx >= n || P.o_col[lo + idx] != target) return;
     const uint32_t b = lo + idx;
     const uint32_t rb = P.rnd[b];
-    if (rb != 0 && rb != r) return;
+    if (rb != 0 && rb < r) return;
     if ((ra == r && a < e) || (rb == r && b < e)) return;  // a smaller-id edge of this round owns it
-    if (ra == 0) {
+    if (ra != r) {
         const uint32_t old = atomicSub(&P.sup[a], 1u);
-        if (old == km2) qnext[atomicAdd(next_count, 1u)] = a;
+        if (old == km2) push_edge(P, a, r + 1);
     }
-    if (rb == 0) {
+    if (rb != r) {
         const uint32_t old = atomicSub(&P.sup[b], 1u);
-        if (old == km2) qnext[atomicAdd(next_count, 1u)] = b;
+        if (old == km2) push_edge(P, b, r + 1);
     }
 }
 
+// Edge e's row walk context: the other endpoint y, the start and length of the shorter row.
+__device__ __forceinline__ void slot_context(const PeelParams& P, uint32_t e, uint32_t* y, uint32_t* base,
+                                             uint32_t* len) {
+    const uint32_t u = P.e_src[e], v = P.o_col[e];
+    const uint32_t lu = P.s_len[u], lv = P.s_len[v];
+    const bool ux = lu <= lv;
+    *y = ux ? v : u;
+    *base = P.s_ptr[ux ? u : v];
+    *len = ux ? lu : lv;
+}
+
 // In-place ordered compaction of the symmetric rows: warps take the short rows [0, big_row),
-// blocks the long rows [big_row, n).  Each step reads before any write of the step, and writes
-// never pass the read position.
-__device__ void compact_rows(const PeelParams& P, uint32_t* warp_cnt) {
+// blocks the long rows [big_row, n).  Entries of edges removed in rounds <= r_done are dropped.
+// Each step reads before any write of the step, and writes never pass the read position.
+__device__ void compact_rows(const PeelParams& P, uint32_t r_done, uint32_t* warp_cnt) {
     const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
     const uint32_t gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -126,7 +152,8 @@ __device__ void compact_rows(const PeelParams& P, uint32_t* warp_cnt) {
             if (i < len) {
                 c = P.s_col[base + i];
                 eid = P.s_eid[base + i];
-                keep = P.rnd[eid] == 0;
+                const uint32_t rr = P.rnd[eid];
+                keep = rr == 0 || rr > r_done;
             }
             const uint32_t ballot = __ballot_sync(kFullMask, keep);
             __syncwarp();
@@ -150,7 +177,8 @@ __device__ void compact_rows(const PeelParams& P, uint32_t* warp_cnt) {
             if (i < len) {
                 c = P.s_col[base + i];
                 eid = P.s_eid[base + i];
-                keep = P.rnd[eid] == 0;
+                const uint32_t rr = P.rnd[eid];
+                keep = rr == 0 || rr > r_done;
             }
             const uint32_t ballot = __ballot_sync(kFullMask, keep);
             if (lane == 0) warp_cnt[warp] = __popc(ballot);
@@ -173,6 +201,15 @@ __device__ void compact_rows(const PeelParams& P, uint32_t* warp_cnt) {
     }
 }
 
+// Collects a level's first frontier from the alive list: support <= thr, queued for round rr.
+__device__ __forceinline__ void collect(const PeelParams& P, const uint32_t* al, uint32_t count, uint32_t thr,
+                                        uint32_t rr, uint64_t tid, uint64_t nthreads) {
+    for (uint64_t i = tid; i < count; i += nthreads) {
+        const uint32_t e = al[i];
+        if (P.sup[e] <= thr) push_edge(P, e, rr);
+    }
+}
+
 __global__ void __launch_bounds__(kPeelThreads, 1) k_peel(PeelParams P) {
     __shared__ uint32_t warp_cnt[kPeelThreads / 32];
     uint32_t* ctrl = P.ctrl;
@@ -184,136 +221,137 @@ __global__ void __launch_bounds__(kPeelThreads, 1) k_peel(PeelParams P) {
     const uint32_t nwarps = (uint32_t)(nthreads >> 5);
     const bool leader = blockIdx.x == 0 && threadIdx.x == 0;
 
+    // phase clock (block 0, thread 0): time from the previous barrier to the end of this one
+    uint64_t phase_ns[6] = {0, 0, 0, 0, 0, 0};
+    uint64_t t_last = leader ? global_ns() : 0;
+    uint32_t compactions = 0;
+#define KT_PHASE(kind)                                   \
+    if (leader) {                                        \
+        const uint64_t now_ = global_ns();               \
+        phase_ns[kind] += now_ - t_last;                 \
+        t_last = now_;                                   \
+    }
+
     for (uint64_t j = tid; j < P.m; j += nthreads) {
         P.rnd[j] = 0;
         P.tr[j] = 0;
         P.alive[0][j] = (uint32_t)j;
     }
     if (!grid_barrier(ctrl, nblocks, P.timeout_ns)) return;
+    KT_PHASE(0)
 
-    uint32_t cur = 0, qc = 0, count = P.m, r = 0, level = 0, k = 3, k_last = 2;
+    uint32_t cur = 0, count = P.m, r = 0, level = 0, k = 3, k_last = 2;
     uint64_t live = P.m, live_at_compaction = P.m;
     for (;;) {
         const uint32_t ls = level & 3;
+        const uint32_t rr = r + 1;  // first round of this level
         if (P.single_k == 0) {
-            // level scan: compact the alive list, minimum support of the survivors
+            // one pass over the alive list: compact it, minimum support, and the frontier of
+            // level k_last+1 (the usual next level); a second pass only if that level is empty
+            const uint32_t kg = k_last + 1;
             if (leader) {
                 const uint32_t z = (level + 2) & 3;
                 ctrl[kPLAlive + z] = 0;
                 ctrl[kPLMin + z] = 0xffffffffu;
-                ctrl[kPLFront + z] = 0;
             }
             const uint32_t* ain = P.alive[cur];
             uint32_t* aout = P.alive[cur ^ 1];
             for (uint64_t i0 = (uint64_t)gwarp * 32; i0 < count; i0 += (uint64_t)nwarps * 32) {
                 const uint64_t i = i0 + lane;
-                uint32_t e = 0, s = 0xffffffffu;
-                bool keep = false;
+                uint32_t e = 0, s = kDead;
                 if (i < count) {
                     e = ain[i];
-                    keep = P.rnd[e] == 0;
-                    if (keep) s = P.sup[e];
+                    s = P.sup[e];
                 }
+                const bool keep = s != kDead;
                 const uint32_t ballot = __ballot_sync(kFullMask, keep);
                 uint32_t base = 0;
                 if (lane == 0 && ballot) base = atomicAdd(ctrl + kPLAlive + ls, __popc(ballot));
                 base = __shfl_sync(kFullMask, base, 0);
-                if (keep) aout[base + __popc(ballot & lanemask_lt())] = e;
+                if (keep) {
+                    aout[base + __popc(ballot & lanemask_lt())] = e;
+                    if (s <= kg - 3) push_edge(P, e, rr);
+                }
                 s = __reduce_min_sync(kFullMask, s);
-                if (lane == 0 && s != 0xffffffffu) atomicMin(ctrl + kPLMin + ls, s);
+                if (lane == 0 && s != kDead) atomicMin(ctrl + kPLMin + ls, s);
             }
             if (!grid_barrier(ctrl, nblocks, P.timeout_ns)) return;
+            KT_PHASE(1)
             count = ld_acquire(ctrl + kPLAlive + ls);
             if (count == 0) break;
-            k = ld_acquire(ctrl + kPLMin + ls) + 3;
             cur ^= 1;
+            k = ld_acquire(ctrl + kPLMin + ls) + 3;
+            if (k != kg) {
+                collect(P, P.alive[cur], count, k - 3, rr, tid, nthreads);
+                if (!grid_barrier(ctrl, nblocks, P.timeout_ns)) return;
+                KT_PHASE(2)
+            }
         } else {
             k = P.single_k;
-            if (leader) ctrl[kPLFront + ls] = 0;
+            collect(P, P.alive[cur], count, k - 3, rr, tid, nthreads);
             if (!grid_barrier(ctrl, nblocks, P.timeout_ns)) return;
+            KT_PHASE(2)
         }
-        // frontier of the level's first round: alive edges with support <= k-3
-        {
-            const uint32_t* al = P.alive[cur];
-            uint32_t* q = P.q[qc];
-            const uint32_t thr = k - 3;
-            for (uint64_t i0 = (uint64_t)gwarp * 32; i0 < count; i0 += (uint64_t)nwarps * 32) {
-                const uint64_t i = i0 + lane;
-                uint32_t e = 0;
-                bool take = false;
-                if (i < count) {
-                    e = al[i];
-                    take = P.sup[e] <= thr;
-                }
-                const uint32_t ballot = __ballot_sync(kFullMask, take);
-                uint32_t base = 0;
-                if (lane == 0 && ballot) base = atomicAdd(ctrl + kPLFront + ls, __popc(ballot));
-                base = __shfl_sync(kFullMask, base, 0);
-                if (take) q[base + __popc(ballot & lanemask_lt())] = e;
-            }
-        }
-        if (!grid_barrier(ctrl, nblocks, P.timeout_ns)) return;
-        uint32_t F = ld_acquire(ctrl + kPLFront + ls);
         const uint32_t km2 = k - 2;
-        while (F) {
+        uint32_t S = ld_acquire(ctrl + kPNext + (rr & 3)), B = ld_acquire(ctrl + kPBigCount + (rr & 3));
+        while (S + B) {
             if (live * 2 < live_at_compaction) {
-                compact_rows(P, warp_cnt);
+                compact_rows(P, r, warp_cnt);
                 if (!grid_barrier(ctrl, nblocks, P.timeout_ns)) return;
+                KT_PHASE(3)
+                ++compactions;
                 live_at_compaction = live;
             }
             ++r;
-            const uint32_t rs = r & 3;
-            // mark
             if (leader) {
                 const uint32_t z = (r + 2) & 3;
                 ctrl[kPNext + z] = 0;
                 ctrl[kPBigCount + z] = 0;
                 if (r < P.cap_rounds) {
-                    P.round_size[r] = F;
+                    P.round_size[r] = S + B;
                     P.round_level[r] = k;
                 }
             }
+            // short rows: one warp per slot, or several warps per slot when slots are few
             {
-                const uint32_t* q = P.q[qc];
-                for (uint64_t i = tid; i < F; i += nthreads) {
+                const uint32_t* q = P.q[r & 1];
+                const uint32_t parts = S >= nwarps ? 1u : min(8u, nwarps / (S ? S : 1));
+                const uint32_t units = S >= nwarps ? S : S * parts;
+                for (uint32_t u = gwarp; u < units; u += nwarps) {
+                    const uint32_t i = u % S, part = u / S;
                     const uint32_t e = q[i];
-                    P.rnd[e] = r;
-                    P.tr[e] = k - 1;
-                    const uint32_t u = P.e_src[e], v = P.o_col[e];
-                    const uint32_t lu = P.s_len[u], lv = P.s_len[v];
-                    const bool ux = lu <= lv;
-                    const uint32_t x = ux ? u : v, len = ux ? lu : lv;
-                    P.fy[i] = ux ? v : u;
-                    P.fbase[i] = P.s_ptr[x];
-                    P.flen[i] = len;
-                    if (len > kLongRow) P.big[atomicAdd(ctrl + kPBigCount + rs, 1u)] = (uint32_t)i;
+                    uint32_t y, base, len;
+                    slot_context(P, e, &y, &base, &len);
+                    if (part == 0 && lane == 0) {
+                        P.tr[e] = k - 1;
+                        P.sup[e] = kDead;
+                    }
+                    for (uint32_t t = part * 32 + lane; t < len; t += parts * 32) peel_entry(P, e, y, base + t, r, km2);
                 }
             }
-            if (!grid_barrier(ctrl, nblocks, P.timeout_ns)) return;
-            // process
+            // long rows: one block per slot, or several blocks per slot when slots are few
             {
-                const uint32_t* q = P.q[qc];
-                uint32_t* qnext = P.q[qc ^ 1];
-                uint32_t* next_count = ctrl + kPNext + rs;
-                for (uint32_t i = gwarp; i < F; i += nwarps) {
-                    const uint32_t len = P.flen[i];
-                    if (len > kLongRow) continue;
-                    const uint32_t e = q[i], y = P.fy[i], base = P.fbase[i];
-                    for (uint32_t t = lane; t < len; t += 32) peel_entry(P, e, y, base + t, r, km2, qnext, next_count);
-                }
-                __syncthreads();
-                const uint32_t nbig = ld_acquire(ctrl + kPBigCount + rs);
-                for (uint32_t j = blockIdx.x; j < nbig; j += nblocks) {
-                    const uint32_t i = P.big[j];
-                    const uint32_t e = q[i], y = P.fy[i], base = P.fbase[i], len = P.flen[i];
-                    for (uint32_t t = threadIdx.x; t < len; t += blockDim.x)
-                        peel_entry(P, e, y, base + t, r, km2, qnext, next_count);
+                const uint32_t* bq = P.big[r & 1];
+                const uint32_t parts = B >= nblocks ? 1u : nblocks / (B ? B : 1);
+                const uint32_t units = B >= nblocks ? B : B * parts;
+                for (uint32_t u = blockIdx.x; u < units; u += nblocks) {
+                    const uint32_t i = u % B, part = u / B;
+                    const uint32_t e = bq[i];
+                    uint32_t y, base, len;
+                    slot_context(P, e, &y, &base, &len);
+                    if (part == 0 && threadIdx.x == 0) {
+                        P.tr[e] = k - 1;
+                        P.sup[e] = kDead;
+                    }
+                    for (uint32_t t = part * blockDim.x + threadIdx.x; t < len; t += parts * blockDim.x)
+                        peel_entry(P, e, y, base + t, r, km2);
                 }
             }
             if (!grid_barrier(ctrl, nblocks, P.timeout_ns)) return;
-            live -= F;
-            F = ld_acquire(ctrl + kPNext + rs);
-            qc ^= 1;
+            KT_PHASE(5)
+            live -= S + B;
+            S = ld_acquire(ctrl + kPNext + ((r + 1) & 3));
+            B = ld_acquire(ctrl + kPBigCount + ((r + 1) & 3));
         }
         ++level;
         k_last = k;
@@ -323,7 +361,13 @@ __global__ void __launch_bounds__(kPeelThreads, 1) k_peel(PeelParams P) {
         ctrl[kPKmax] = P.single_k ? 0 : k_last - 1;
         ctrl[kPRounds] = r;
         ctrl[kPLevels] = level;
+        ctrl[kPCompactions] = compactions;
+        for (int i = 0; i < 6; ++i) {
+            ctrl[kPPhaseNs + 2 * i] = (uint32_t)phase_ns[i];
+            ctrl[kPPhaseNs + 2 * i + 1] = (uint32_t)(phase_ns[i] >> 32);
+        }
     }
+#undef KT_PHASE
 }
 
 // A barrier that cannot complete (it expects one block more than the grid has): every wait
@@ -388,10 +432,8 @@ int launch_peel(kt_engine* e, uint32_t single_k) {
     P.alive[1] = e->alive1;
     P.q[0] = e->q0;
     P.q[1] = e->q1;
-    P.fy = e->fy;
-    P.fbase = e->fbase;
-    P.flen = e->flen;
-    P.big = e->big;
+    P.big[0] = e->fy;  // the two long-row queues reuse the per-slot scratch arrays
+    P.big[1] = e->flen;
     P.ctrl = e->ctrl;
     P.round_size = e->round_size;
     P.round_level = e->round_level;
@@ -483,6 +525,8 @@ int emit_keep(kt_engine* e, uint8_t* d_keep) {
 int finish_stats(kt_engine* e) {
     if (e->stats_ready) return KT_OK;
     if (e->m == 0 || e->peel_mode == 2) {
+        e->stats.compactions = 0;
+        for (int i = 0; i < 6; ++i) e->stats.peel_phase_ms[i] = 0;
         e->stats.k_max = 0;
         e->stats.num_rounds = e->stats.num_levels = e->stats.plain_passes = 0;
         e->stats.plain_alive_sum = 0;
@@ -500,6 +544,10 @@ int finish_stats(kt_engine* e) {
     e->stats.k_max = m ? (e->peel_mode == 0 ? e->h_ctrl[kPKmax] : 0) : 0;
     e->stats.num_rounds = m ? e->h_ctrl[kPRounds] : 0;
     e->stats.num_levels = m ? e->h_ctrl[kPLevels] : 0;
+    e->stats.compactions = e->h_ctrl[kPCompactions];
+    for (int i = 0; i < 6; ++i)
+        e->stats.peel_phase_ms[i] =
+            (float)(((uint64_t)e->h_ctrl[kPPhaseNs + 2 * i + 1] << 32 | e->h_ctrl[kPPhaseNs + 2 * i]) * 1e-6);
     e->stats.plain_passes = 0;
     e->stats.plain_alive_sum = 0;
     const uint32_t R = e->stats.num_rounds;

@@ -66,10 +66,15 @@ class Stats(ctypes.Structure):
                 ("num_levels", ctypes.c_uint32), ("num_rounds", ctypes.c_uint32), ("triangles", ctypes.c_uint64),
                 ("plain_alive_sum", ctypes.c_uint64), ("plain_passes", ctypes.c_uint32),
                 ("kernel_launches", ctypes.c_uint64), ("last_ms", ctypes.c_float),
-                ("build_ms", ctypes.c_float), ("support_ms", ctypes.c_float), ("peel_ms", ctypes.c_float)]
+                ("build_ms", ctypes.c_float), ("support_ms", ctypes.c_float), ("peel_ms", ctypes.c_float),
+                ("compactions", ctypes.c_uint32), ("peel_phase_ms", ctypes.c_float * 6)]
+
+    PHASES = ("init", "level_scan", "collect", "compaction", "mark", "process")
 
     def as_dict(self) -> dict:
-        return {f: getattr(self, f) for f, _ in self._fields_}
+        d = {f: getattr(self, f) for f, _ in self._fields_}
+        d["peel_phase_ms"] = dict(zip(self.PHASES, list(self.peel_phase_ms)))
+        return d
 
 
 _LIB = None
