@@ -48,7 +48,8 @@ typedef enum kt_status {
     KT_ERR_MISMATCH = 10,       /* verify: edge count or edge set differs (verify.cu:18,28-29)  */
     KT_ERR_TIMEOUT = 11,        /* a bounded device-side wait expired; the device stays usable */
     KT_ERR_NO_DEVICE = 12,
-    KT_ERR_TOO_LARGE = 13       /* graph exceeds the 32-bit index space of the layout          */
+    KT_ERR_TOO_LARGE = 13,      /* graph exceeds the 32-bit index space of the layout          */
+    KT_ERR_INTERNAL = 14        /* a device-side consistency bound was exceeded (a bug)        */
 } kt_status;
 
 /* ---- graph and configuration structs -------------------------------------------------- */

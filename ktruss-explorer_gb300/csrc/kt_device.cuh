@@ -18,6 +18,7 @@ enum : uint32_t {
     kErrDuplicate = 1u << 2,   // the same (src, dst) entry twice
     kErrAsymmetric = 1u << 3,  // (u, v) present without (v, u)
     kErrTimeout = 1u << 4,     // a bounded grid-barrier wait expired
+    kErrRunaway = 1u << 5,     // the peel loop exceeded its round or level bound
 };
 
 // Layout of the device control block (uint32 words unless noted).

@@ -51,6 +51,7 @@ const char* kt_status_string(int s) {
         case KT_ERR_TIMEOUT: return "device wait timed out";
         case KT_ERR_NO_DEVICE: return "no CUDA device";
         case KT_ERR_TOO_LARGE: return "graph too large";
+        case KT_ERR_INTERNAL: return "internal consistency check failed";
         default: return "unknown status";
     }
 }

@@ -240,58 +240,21 @@ __global__ void __launch_bounds__(kPeelThreads, 1) k_peel(PeelParams P) {
     if (!grid_barrier(ctrl, nblocks, P.timeout_ns)) return;
     KT_PHASE(0)
 
-    uint32_t cur = 0, count = P.m, r = 0, level = 0, k = 3, k_last = 2;
+    // r: stamp of the last round run.  A level's first round skips one stamp: the blocks still
+    // reading the previous level's exit test look at ring slot (r+1) & 3, so the new level's
+    // first frontier goes to slot (r+2) & 3.  `rounds` counts the rounds actually run.
+    uint32_t cur = 0, count = P.m, r = 0, rounds = 0, level = 0, k = 3, k_last = 2;
     uint64_t live = P.m, live_at_compaction = P.m;
+    const uint64_t max_stamp = 2ull * P.m + 8;
     for (;;) {
         const uint32_t ls = level & 3;
-        const uint32_t rr = r + 1;  // first round of this level
-        if (P.single_k == 0) {
-            // one pass over the alive list: compact it, minimum support, and the frontier of
-            // level k_last+1 (the usual next level); a second pass only if that level is empty
-            const uint32_t kg = k_last + 1;
-            if (leader) {
-                const uint32_t z = (level + 2) & 3;
-                ctrl[kPLAlive + z] = 0;
-                ctrl[kPLMin + z] = 0xffffffffu;
-            }
-            const uint32_t* ain = P.alive[cur];
-            uint32_t* aout = P.alive[cur ^ 1];
-            for (uint64_t i0 = (uint64_t)gwarp * 32; i0 < count; i0 += (uint64_t)nwarps * 32) {
-                const uint64_t i = i0 + lane;
-                uint32_t e = 0, s = kDead;
-                if (i < count) {
-                    e = ain[i];
-                    s = P.sup[e];
-                }
-                const bool keep = s != kDead;
-                const uint32_t ballot = __ballot_sync(kFullMask, keep);
-                uint32_t base = 0;
-                if (lane == 0 && ballot) base = atomicAdd(ctrl + kPLAlive + ls, __popc(ballot));
-                base = __shfl_sync(kFullMask, base, 0);
-                if (keep) {
-                    aout[base + __popc(ballot & lanemask_lt())] = e;
-                    if (s <= kg - 3) push_edge(P, e, rr);
-                }
-                s = __reduce_min_sync(kFullMask, s);
-                if (lane == 0 && s != kDead) atomicMin(ctrl + kPLMin + ls, s);
-            }
-            if (!grid_barrier(ctrl, nblocks, P.timeout_ns)) return;
-            KT_PHASE(1)
-            count = ld_acquire(ctrl + kPLAlive + ls);
-            if (count == 0) break;
-            cur ^= 1;
-            k = ld_acquire(ctrl + kPLMin + ls) + 3;
-            if (k != kg) {
-                collect(P, P.alive[cur], count, k - 3, rr, tid, nthreads);
-                if (!grid_barrier(ctrl, nblocks, P.timeout_ns)) return;
-                KT_PHASE(2)
-            }
-        } else {
-            k = P.single_k;
-            collect(P, P.alive[cur], count, k - 3, rr, tid, nthreads);
-            if (!grid_barrier(ctrl, nblocks, P.timeout_ns)) return;
-            KT_PHASE(2)
+        r += 1;                     // skipped stamp
+        const uint32_t rr = r + 1;  // stamp of this level's first round
+        if (level > P.m + 1 || rr > max_stamp) {
+            if (leader) atomicOr(ctrl + kCtrlError, kErrRunaway);
+            return;
         }
+        if (leader) ctrl[kPNext + ((rr + 1) & 3)] = ctrl[kPBigCount + ((rr + 1) & 3)] = 0;
         const uint32_t km2 = k - 2;
         uint32_t S = ld_acquire(ctrl + kPNext + (rr & 3)), B = ld_acquire(ctrl + kPBigCount + (rr & 3));
         while (S + B) {
@@ -303,13 +266,18 @@ __global__ void __launch_bounds__(kPeelThreads, 1) k_peel(PeelParams P) {
                 live_at_compaction = live;
             }
             ++r;
+            ++rounds;
+            if (r > max_stamp) {
+                if (leader) atomicOr(ctrl + kCtrlError, kErrRunaway);
+                return;
+            }
             if (leader) {
                 const uint32_t z = (r + 2) & 3;
                 ctrl[kPNext + z] = 0;
                 ctrl[kPBigCount + z] = 0;
-                if (r < P.cap_rounds) {
-                    P.round_size[r] = S + B;
-                    P.round_level[r] = k;
+                if (rounds < P.cap_rounds) {
+                    P.round_size[rounds] = S + B;
+                    P.round_level[rounds] = k;
                 }
             }
             // short rows: one warp per slot, or several warps per slot when slots are few
@@ -359,7 +327,7 @@ __global__ void __launch_bounds__(kPeelThreads, 1) k_peel(PeelParams P) {
     }
     if (leader) {
         ctrl[kPKmax] = P.single_k ? 0 : k_last - 1;
-        ctrl[kPRounds] = r;
+        ctrl[kPRounds] = rounds;
         ctrl[kPLevels] = level;
         ctrl[kPCompactions] = compactions;
         for (int i = 0; i < 6; ++i) {
@@ -539,6 +507,7 @@ int finish_stats(kt_engine* e) {
     if (rc) return rc;
     const uint32_t err = e->h_ctrl[kCtrlError];
     if (err & kErrTimeout) return fail(KT_ERR_TIMEOUT, "a grid barrier wait of the peel kernel expired");
+    if (err & kErrRunaway) return fail(KT_ERR_INTERNAL, "the peel kernel exceeded its round or level bound");
     const uint64_t m = e->m;
     e->stats.triangles = ((uint64_t)e->h_ctrl[kCtrlTriHi] << 32 | e->h_ctrl[kCtrlTriLo]) / 3;
     e->stats.k_max = m ? (e->peel_mode == 0 ? e->h_ctrl[kPKmax] : 0) : 0;
@@ -562,6 +531,7 @@ int finish_stats(kt_engine* e) {
         uint32_t next_k = 3;
         for (uint32_t r = 1; r <= R;) {
             const uint32_t k = lvl[r];
+            if (k < next_k || k > e->stats.k_max + 1) return fail(KT_ERR_INTERNAL, "inconsistent round log");
             for (uint32_t kk = next_k > 4 ? next_k : 4; kk < k; ++kk) { passes++; alive_sum += alive; }
             while (r <= R && lvl[r] == k) {
                 if (k >= 4) { passes++; alive_sum += alive; }

@@ -32,7 +32,7 @@ KT_OK = 0
 STATUS_NAMES = {0: "KT_OK", 1: "KT_ERR_INVALID_ARG", 2: "KT_ERR_SELF_LOOP", 3: "KT_ERR_NOT_SYMMETRIC",
                 4: "KT_ERR_CAPACITY", 5: "KT_ERR_UNSUPPORTED", 6: "KT_ERR_CUDA", 7: "KT_ERR_DEVICE_ALLOC",
                 8: "KT_ERR_HOST_ALLOC", 9: "KT_ERR_IO", 10: "KT_ERR_MISMATCH", 11: "KT_ERR_TIMEOUT",
-                12: "KT_ERR_NO_DEVICE", 13: "KT_ERR_TOO_LARGE"}
+                12: "KT_ERR_NO_DEVICE", 13: "KT_ERR_TOO_LARGE", 14: "KT_ERR_INTERNAL"}
 
 
 class KtrussError(RuntimeError):
