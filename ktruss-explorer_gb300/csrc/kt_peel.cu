@@ -255,6 +255,53 @@ __global__ void __launch_bounds__(kPeelThreads, 1) k_peel(PeelParams P) {
             return;
         }
         if (leader) ctrl[kPNext + ((rr + 1) & 3)] = ctrl[kPBigCount + ((rr + 1) & 3)] = 0;
+        if (P.single_k == 0) {
+            // one pass over the alive list: compact it, minimum support, and the frontier of
+            // level k_last+1 (the usual next level); a second pass only if that level is empty
+            const uint32_t kg = k_last + 1;
+            if (leader) {
+                const uint32_t z = (level + 2) & 3;
+                ctrl[kPLAlive + z] = 0;
+                ctrl[kPLMin + z] = 0xffffffffu;
+            }
+            const uint32_t* ain = P.alive[cur];
+            uint32_t* aout = P.alive[cur ^ 1];
+            for (uint64_t i0 = (uint64_t)gwarp * 32; i0 < count; i0 += (uint64_t)nwarps * 32) {
+                const uint64_t i = i0 + lane;
+                uint32_t e = 0, s = kDead;
+                if (i < count) {
+                    e = ain[i];
+                    s = P.sup[e];
+                }
+                const bool keep = s != kDead;
+                const uint32_t ballot = __ballot_sync(kFullMask, keep);
+                uint32_t base = 0;
+                if (lane == 0 && ballot) base = atomicAdd(ctrl + kPLAlive + ls, __popc(ballot));
+                base = __shfl_sync(kFullMask, base, 0);
+                if (keep) {
+                    aout[base + __popc(ballot & lanemask_lt())] = e;
+                    if (s <= kg - 3) push_edge(P, e, rr);
+                }
+                s = __reduce_min_sync(kFullMask, s);
+                if (lane == 0 && s != kDead) atomicMin(ctrl + kPLMin + ls, s);
+            }
+            if (!grid_barrier(ctrl, nblocks, P.timeout_ns)) return;
+            KT_PHASE(1)
+            count = ld_acquire(ctrl + kPLAlive + ls);
+            if (count == 0) break;
+            cur ^= 1;
+            k = ld_acquire(ctrl + kPLMin + ls) + 3;
+            if (k != kg) {
+                collect(P, P.alive[cur], count, k - 3, rr, tid, nthreads);
+                if (!grid_barrier(ctrl, nblocks, P.timeout_ns)) return;
+                KT_PHASE(2)
+            }
+        } else {
+            k = P.single_k;
+            collect(P, P.alive[cur], count, k - 3, rr, tid, nthreads);
+            if (!grid_barrier(ctrl, nblocks, P.timeout_ns)) return;
+            KT_PHASE(2)
+        }
         const uint32_t km2 = k - 2;
         uint32_t S = ld_acquire(ctrl + kPNext + (rr & 3)), B = ld_acquire(ctrl + kPBigCount + (rr & 3));
         while (S + B) {
