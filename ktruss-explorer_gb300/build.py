@@ -25,7 +25,7 @@ INCLUDE = os.path.join(ROOT, "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
-              "--expt-relaxed-constexpr"] + ARCH
+              "--expt-relaxed-constexpr"] + ARCH + os.environ.get("KT_NVCC_FLAGS", "").split()
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-unused-function"]
 
 LIB_SOURCES = ["kt_host.cpp", "kt_gen.cpp", "kt_sort.cu", "kt_build.cu", "kt_support.cu", "kt_peel.cu",

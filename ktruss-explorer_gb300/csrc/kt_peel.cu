@@ -13,8 +13,8 @@
 // edges are still alive or removed in round r is destroyed once: the removed edge with the
 // smallest id among the triangle's round-r edges decrements each surviving edge by one.  A
 // decrement that takes an edge from k-2 to k-3 pushes it onto the next round's frontier, so
-// frontiers are built without scans.  A new level starts from a warp-ballot compaction of the
-// alive-edge list that also finds the minimum support, so empty levels are skipped (k jumps to
+// frontiers are built without scans.  A new level starts from one coalesced pass over the
+// support array that also finds the minimum support, so empty levels are skipped (k jumps to
 // min+3).
 //
 // One round is one phase followed by one grid barrier: warps walk the frontier edges' short
@@ -42,8 +42,18 @@ namespace kt {
 namespace {
 
 constexpr int kThreads = 256;          // helper kernels
-constexpr int kPeelThreads = 1024;     // persistent kernel: one block per SM
+#ifndef KT_PEEL_THREADS
+#define KT_PEEL_THREADS 1024
+#endif
+#ifndef KT_PEEL_BATCH
+#define KT_PEEL_BATCH 2
+#endif
+constexpr int kPeelThreads = KT_PEEL_THREADS;  // persistent kernel: one block per SM
 constexpr uint32_t kLongRow = 256;     // rows longer than this are walked by a whole block
+constexpr int kBatch = KT_PEEL_BATCH;  // row entries in flight per thread
+// Rows are compacted once the alive edges fall below this fraction (num/den) of the count at
+// the last compaction.
+constexpr uint64_t kCompactNum = 17, kCompactDen = 20;
 constexpr uint64_t kPeelTimeoutNs = 10ull * 1000 * 1000 * 1000;
 
 inline uint32_t grid_for(uint64_t n, int threads = kThreads) {
@@ -62,7 +72,6 @@ struct PeelParams {
     uint32_t* sup;
     uint32_t* rnd;
     uint32_t* tr;
-    uint32_t* alive[2];
     uint32_t* q[2];    // frontier slots with short rows, by round parity
     uint32_t* big[2];  // frontier slots with long rows, by round parity
     uint32_t* ctrl;
@@ -87,39 +96,86 @@ __device__ __forceinline__ void push_edge(const PeelParams& P, uint32_t e, uint3
     else P.q[rr & 1][atomicAdd(P.ctrl + kPNext + slot, 1u)] = e;
 }
 
-// One entry of a removed edge's shorter row: neighbour w of x at row position p.  Edge states
-// during round r: rnd 0 = alive, r+1 = alive but queued for the next round, r = removed in this
-// round, 1..r-1 = removed earlier.
-__device__ __forceinline__ void peel_entry(const PeelParams& P, uint32_t e, uint32_t y, uint32_t p, uint32_t r,
-                                           uint32_t km2) {
-    const uint32_t w = P.s_col[p];
-    if (w == y) return;
-    const uint32_t a = P.s_eid[p];
-    const uint32_t ra = P.rnd[a];
-    if (ra != 0 && ra < r) return;  // (x,w) removed in an earlier round: triangle already gone
-    uint32_t lo, n, target;
-    if (w > y) {
-        lo = P.o_ptr[y];
-        n = P.o_ptr[y + 1] - lo;
-        target = w;
-    } else {
-        lo = P.o_ptr[w];
-        n = P.o_ptr[w + 1] - lo;
-        target = y;
+// Entries of a removed edge e's shorter row (vertex x), NB at a time per thread so that the
+// memory chains of different entries overlap: positions base + t0 + j*step, j < NB, below
+// base + len.  For a neighbour w of x, edge (x,w) is s_eid at the entry and edge (y,w) is found
+// by a binary search in an oriented row (w in N+(y) if w > y, else y in N+(w)); the NB searches
+// advance in lockstep.  Edge states during round r: rnd 0 = alive, r+1 = alive but queued for
+// the next round, r = removed in this round, 1..r-1 = removed earlier.  A triangle is skipped if
+// one of its edges was removed earlier or if a smaller-id edge of this round owns it; otherwise
+// each surviving edge loses one support, and an edge whose support falls from k-2 to k-3 is
+// queued for round r+1.
+template <int NB>
+__device__ __forceinline__ void peel_entries(const PeelParams& P, uint32_t e, uint32_t y, uint32_t base, uint32_t len,
+                                             uint32_t t0, uint32_t step, uint32_t r, uint32_t km2) {
+    uint32_t a[NB], lo[NB], n[NB], end[NB], tgt[NB];
+    bool act[NB];
+#pragma unroll
+    for (int j = 0; j < NB; ++j) {
+        const uint32_t t = t0 + (uint32_t)j * step;
+        act[j] = t < len;
+        uint32_t w = y;
+        if (act[j]) {
+            w = P.s_col[base + t];
+            a[j] = P.s_eid[base + t];
+        }
+        act[j] = act[j] && w != y;
+        if (act[j]) {
+            const uint32_t row = w > y ? y : w;
+            tgt[j] = w > y ? w : y;
+            lo[j] = P.o_ptr[row];
+            end[j] = P.o_ptr[row + 1];
+            n[j] = end[j] - lo[j];
+        }
     }
-    const uint32_t idx = lower_bound_u32(P.o_col + lo, n, target);
-    if (idx >= n || P.o_col[lo + idx] != target) return;
-    const uint32_t b = lo + idx;
-    const uint32_t rb = P.rnd[b];
-    if (rb != 0 && rb < r) return;
-    if ((ra == r && a < e) || (rb == r && b < e)) return;  // a smaller-id edge of this round owns it
-    if (ra != r) {
-        const uint32_t old = atomicSub(&P.sup[a], 1u);
-        if (old == km2) push_edge(P, a, r + 1);
+    uint32_t ra[NB];
+#pragma unroll
+    for (int j = 0; j < NB; ++j) {
+        if (act[j]) {
+            ra[j] = P.rnd[a[j]];
+            if (ra[j] != 0 && ra[j] < r) act[j] = false;  // (x,w) removed earlier: triangle gone
+        }
+        if (!act[j]) n[j] = 0;
     }
-    if (rb != r) {
-        const uint32_t old = atomicSub(&P.sup[b], 1u);
-        if (old == km2) push_edge(P, b, r + 1);
+    // lockstep lower bounds
+    bool more = true;
+    while (more) {
+        more = false;
+#pragma unroll
+        for (int j = 0; j < NB; ++j) {
+            if (n[j] > 0) {
+                const uint32_t half = n[j] >> 1;
+                if (__ldg(P.o_col + lo[j] + half) < tgt[j]) {
+                    lo[j] += half + 1;
+                    n[j] -= half + 1;
+                } else {
+                    n[j] = half;
+                }
+                more = more || n[j] > 0;
+            }
+        }
+    }
+    uint32_t rb[NB];
+#pragma unroll
+    for (int j = 0; j < NB; ++j) {
+        // lo is the lower bound: the edge exists only if it is inside the row and matches
+        if (act[j]) act[j] = lo[j] < end[j] && __ldg(P.o_col + lo[j]) == tgt[j];
+        if (act[j]) rb[j] = P.rnd[lo[j]];
+    }
+#pragma unroll
+    for (int j = 0; j < NB; ++j) {
+        if (!act[j]) continue;
+        const uint32_t b = lo[j];
+        if (rb[j] != 0 && rb[j] < r) continue;
+        if ((ra[j] == r && a[j] < e) || (rb[j] == r && b < e)) continue;  // owned by a smaller id
+        if (ra[j] != r) {
+            const uint32_t old = atomicSub(&P.sup[a[j]], 1u);
+            if (old == km2) push_edge(P, a[j], r + 1);
+        }
+        if (rb[j] != r) {
+            const uint32_t old = atomicSub(&P.sup[b], 1u);
+            if (old == km2) push_edge(P, b, r + 1);
+        }
     }
 }
 
@@ -201,13 +257,12 @@ __device__ void compact_rows(const PeelParams& P, uint32_t r_done, uint32_t* war
     }
 }
 
-// Collects a level's first frontier from the alive list: support <= thr, queued for round rr.
-__device__ __forceinline__ void collect(const PeelParams& P, const uint32_t* al, uint32_t count, uint32_t thr,
-                                        uint32_t rr, uint64_t tid, uint64_t nthreads) {
-    for (uint64_t i = tid; i < count; i += nthreads) {
-        const uint32_t e = al[i];
-        if (P.sup[e] <= thr) push_edge(P, e, rr);
-    }
+// Collects a level's first frontier: alive edges with support <= thr, queued for round rr
+// (removed edges hold kDead and never qualify).
+__device__ __forceinline__ void collect(const PeelParams& P, uint32_t thr, uint32_t rr, uint64_t tid,
+                                        uint64_t nthreads) {
+    for (uint64_t j = tid; j < P.m; j += nthreads)
+        if (P.sup[j] <= thr) push_edge(P, (uint32_t)j, rr);
 }
 
 __global__ void __launch_bounds__(kPeelThreads, 1) k_peel(PeelParams P) {
@@ -235,7 +290,6 @@ __global__ void __launch_bounds__(kPeelThreads, 1) k_peel(PeelParams P) {
     for (uint64_t j = tid; j < P.m; j += nthreads) {
         P.rnd[j] = 0;
         P.tr[j] = 0;
-        P.alive[0][j] = (uint32_t)j;
     }
     if (!grid_barrier(ctrl, nblocks, P.timeout_ns)) return;
     KT_PHASE(0)
@@ -243,7 +297,7 @@ __global__ void __launch_bounds__(kPeelThreads, 1) k_peel(PeelParams P) {
     // r: stamp of the last round run.  A level's first round skips one stamp: the blocks still
     // reading the previous level's exit test look at ring slot (r+1) & 3, so the new level's
     // first frontier goes to slot (r+2) & 3.  `rounds` counts the rounds actually run.
-    uint32_t cur = 0, count = P.m, r = 0, rounds = 0, level = 0, k = 3, k_last = 2;
+    uint32_t r = 0, rounds = 0, level = 0, k = 3, k_last = 2;
     uint64_t live = P.m, live_at_compaction = P.m;
     const uint64_t max_stamp = 2ull * P.m + 8;
     for (;;) {
@@ -264,48 +318,41 @@ __global__ void __launch_bounds__(kPeelThreads, 1) k_peel(PeelParams P) {
                 ctrl[kPLAlive + z] = 0;
                 ctrl[kPLMin + z] = 0xffffffffu;
             }
-            const uint32_t* ain = P.alive[cur];
-            uint32_t* aout = P.alive[cur ^ 1];
-            for (uint64_t i0 = (uint64_t)gwarp * 32; i0 < count; i0 += (uint64_t)nwarps * 32) {
-                const uint64_t i = i0 + lane;
-                uint32_t e = 0, s = kDead;
-                if (i < count) {
-                    e = ain[i];
-                    s = P.sup[e];
+            // stream the whole support array (coalesced; removed edges hold kDead)
+            uint32_t n_alive = 0, mn = kDead;
+            for (uint64_t j = tid; j < P.m; j += nthreads) {
+                const uint32_t s = P.sup[j];
+                if (s != kDead) {
+                    ++n_alive;
+                    mn = s < mn ? s : mn;
+                    if (s <= kg - 3) push_edge(P, (uint32_t)j, rr);
                 }
-                const bool keep = s != kDead;
-                const uint32_t ballot = __ballot_sync(kFullMask, keep);
-                uint32_t base = 0;
-                if (lane == 0 && ballot) base = atomicAdd(ctrl + kPLAlive + ls, __popc(ballot));
-                base = __shfl_sync(kFullMask, base, 0);
-                if (keep) {
-                    aout[base + __popc(ballot & lanemask_lt())] = e;
-                    if (s <= kg - 3) push_edge(P, e, rr);
-                }
-                s = __reduce_min_sync(kFullMask, s);
-                if (lane == 0 && s != kDead) atomicMin(ctrl + kPLMin + ls, s);
+            }
+            n_alive = __reduce_add_sync(kFullMask, n_alive);
+            mn = __reduce_min_sync(kFullMask, mn);
+            if (lane == 0) {
+                if (n_alive) atomicAdd(ctrl + kPLAlive + ls, n_alive);
+                if (mn != kDead) atomicMin(ctrl + kPLMin + ls, mn);
             }
             if (!grid_barrier(ctrl, nblocks, P.timeout_ns)) return;
             KT_PHASE(1)
-            count = ld_acquire(ctrl + kPLAlive + ls);
-            if (count == 0) break;
-            cur ^= 1;
+            if (ld_acquire(ctrl + kPLAlive + ls) == 0) break;
             k = ld_acquire(ctrl + kPLMin + ls) + 3;
             if (k != kg) {
-                collect(P, P.alive[cur], count, k - 3, rr, tid, nthreads);
+                collect(P, k - 3, rr, tid, nthreads);
                 if (!grid_barrier(ctrl, nblocks, P.timeout_ns)) return;
                 KT_PHASE(2)
             }
         } else {
             k = P.single_k;
-            collect(P, P.alive[cur], count, k - 3, rr, tid, nthreads);
+            collect(P, k - 3, rr, tid, nthreads);
             if (!grid_barrier(ctrl, nblocks, P.timeout_ns)) return;
             KT_PHASE(2)
         }
         const uint32_t km2 = k - 2;
         uint32_t S = ld_acquire(ctrl + kPNext + (rr & 3)), B = ld_acquire(ctrl + kPBigCount + (rr & 3));
         while (S + B) {
-            if (live * 2 < live_at_compaction) {
+            if (live * kCompactDen < live_at_compaction * kCompactNum) {
                 compact_rows(P, r, warp_cnt);
                 if (!grid_barrier(ctrl, nblocks, P.timeout_ns)) return;
                 KT_PHASE(3)
@@ -341,7 +388,8 @@ __global__ void __launch_bounds__(kPeelThreads, 1) k_peel(PeelParams P) {
                         P.tr[e] = k - 1;
                         P.sup[e] = kDead;
                     }
-                    for (uint32_t t = part * 32 + lane; t < len; t += parts * 32) peel_entry(P, e, y, base + t, r, km2);
+                    for (uint32_t t = part * 32 + lane; t < len; t += parts * 32 * kBatch)
+                        peel_entries<kBatch>(P, e, y, base, len, t, parts * 32, r, km2);
                 }
             }
             // long rows: one block per slot, or several blocks per slot when slots are few
@@ -358,8 +406,8 @@ __global__ void __launch_bounds__(kPeelThreads, 1) k_peel(PeelParams P) {
                         P.tr[e] = k - 1;
                         P.sup[e] = kDead;
                     }
-                    for (uint32_t t = part * blockDim.x + threadIdx.x; t < len; t += parts * blockDim.x)
-                        peel_entry(P, e, y, base + t, r, km2);
+                    for (uint32_t t = part * blockDim.x + threadIdx.x; t < len; t += parts * blockDim.x * kBatch)
+                        peel_entries<kBatch>(P, e, y, base, len, t, parts * blockDim.x, r, km2);
                 }
             }
             if (!grid_barrier(ctrl, nblocks, P.timeout_ns)) return;
@@ -443,8 +491,6 @@ int launch_peel(kt_engine* e, uint32_t single_k) {
     P.sup = e->sup;
     P.rnd = e->rnd;
     P.tr = e->tr;
-    P.alive[0] = e->alive0;
-    P.alive[1] = e->alive1;
     P.q[0] = e->q0;
     P.q[1] = e->q1;
     P.big[0] = e->fy;  // the two long-row queues reuse the per-slot scratch arrays
