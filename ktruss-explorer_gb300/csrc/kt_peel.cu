@@ -46,7 +46,7 @@ constexpr int kThreads = 256;          // helper kernels
 #define KT_PEEL_THREADS 1024
 #endif
 #ifndef KT_PEEL_BATCH
-#define KT_PEEL_BATCH 2
+#define KT_PEEL_BATCH 1
 #endif
 constexpr int kPeelThreads = KT_PEEL_THREADS;  // persistent kernel: one block per SM
 constexpr uint32_t kLongRow = 256;     // rows longer than this are walked by a whole block
@@ -85,34 +85,50 @@ struct PeelParams {
 
 constexpr uint32_t kDead = 0xffffffffu;  // support of a removed edge
 
-// Queues an edge for round rr: stamps it and files it by the length of its shorter row
-// (a scheduling hint; the row is measured again when the round runs).
-__device__ __forceinline__ void push_edge(const PeelParams& P, uint32_t e, uint32_t rr) {
-    P.rnd[e] = rr;
-    const uint32_t lu = P.s_len[P.e_src[e]], lv = P.s_len[P.o_col[e]];
-    const uint32_t len = lu < lv ? lu : lv;
-    const uint32_t slot = rr & 3;
-    if (len > kLongRow) P.big[rr & 1][atomicAdd(P.ctrl + kPBigCount + slot, 1u)] = e;
-    else P.q[rr & 1][atomicAdd(P.ctrl + kPNext + slot, 1u)] = e;
+// Queues edge e for round rr if `take`: stamps it and files it by the length of its shorter row
+// (a scheduling hint; the row is measured again when the round runs).  Called by all 32 lanes
+// of a warp together; the queue slots are claimed with one atomic per queue per warp.
+__device__ __forceinline__ void push_edges(const PeelParams& P, uint32_t e, bool take, uint32_t rr) {
+    bool big = false;
+    if (take) {
+        P.rnd[e] = rr;
+        const uint32_t lu = P.s_len[P.e_src[e]], lv = P.s_len[P.o_col[e]];
+        big = (lu < lv ? lu : lv) > kLongRow;
+    }
+    const uint32_t ms = __ballot_sync(kFullMask, take && !big), mb = __ballot_sync(kFullMask, take && big);
+    if (!(ms | mb)) return;
+    const uint32_t lane = lane_id(), slot = rr & 3;
+    uint32_t bs = 0, bb = 0;
+    if (lane == 0) {
+        if (ms) bs = atomicAdd(P.ctrl + kPNext + slot, __popc(ms));
+        if (mb) bb = atomicAdd(P.ctrl + kPBigCount + slot, __popc(mb));
+    }
+    bs = __shfl_sync(kFullMask, bs, 0);
+    bb = __shfl_sync(kFullMask, bb, 0);
+    if (take) {
+        if (big) P.big[rr & 1][bb + __popc(mb & lanemask_lt())] = e;
+        else P.q[rr & 1][bs + __popc(ms & lanemask_lt())] = e;
+    }
 }
 
-// Entries of a removed edge e's shorter row (vertex x), NB at a time per thread so that the
-// memory chains of different entries overlap: positions base + t0 + j*step, j < NB, below
-// base + len.  For a neighbour w of x, edge (x,w) is s_eid at the entry and edge (y,w) is found
-// by a binary search in an oriented row (w in N+(y) if w > y, else y in N+(w)); the NB searches
-// advance in lockstep.  Edge states during round r: rnd 0 = alive, r+1 = alive but queued for
-// the next round, r = removed in this round, 1..r-1 = removed earlier.  A triangle is skipped if
-// one of its edges was removed earlier or if a smaller-id edge of this round owns it; otherwise
-// each surviving edge loses one support, and an edge whose support falls from k-2 to k-3 is
-// queued for round r+1.
+// Entries of a removed edge e's shorter row (vertex x): called by all 32 lanes of a warp
+// together; lane l handles positions base + t0 + l + j*step (j < NB) that are below base + len,
+// so that the memory chains of different entries overlap.  For a neighbour w of x, edge (x,w) is
+// s_eid at the entry and edge (y,w) is found by a binary search in an oriented row (w in N+(y)
+// if w > y, else y in N+(w)); the NB searches advance in lockstep.  Edge states during round r:
+// rnd 0 = alive, r+1 = alive but queued for the next round, r = removed in this round,
+// 1..r-1 = removed earlier.  A triangle is skipped if one of its edges was removed earlier or if
+// a smaller-id edge of this round owns it; otherwise each surviving edge loses one support, and
+// an edge whose support falls from k-2 to k-3 is queued for round r+1.
 template <int NB>
 __device__ __forceinline__ void peel_entries(const PeelParams& P, uint32_t e, uint32_t y, uint32_t base, uint32_t len,
                                              uint32_t t0, uint32_t step, uint32_t r, uint32_t km2) {
+    const uint32_t lane = lane_id();
     uint32_t a[NB], lo[NB], n[NB], end[NB], tgt[NB];
     bool act[NB];
 #pragma unroll
     for (int j = 0; j < NB; ++j) {
-        const uint32_t t = t0 + (uint32_t)j * step;
+        const uint32_t t = t0 + lane + (uint32_t)j * step;
         act[j] = t < len;
         uint32_t w = y;
         if (act[j]) {
@@ -155,27 +171,22 @@ __device__ __forceinline__ void peel_entries(const PeelParams& P, uint32_t e, ui
             }
         }
     }
-    uint32_t rb[NB];
 #pragma unroll
     for (int j = 0; j < NB; ++j) {
         // lo is the lower bound: the edge exists only if it is inside the row and matches
         if (act[j]) act[j] = lo[j] < end[j] && __ldg(P.o_col + lo[j]) == tgt[j];
-        if (act[j]) rb[j] = P.rnd[lo[j]];
-    }
-#pragma unroll
-    for (int j = 0; j < NB; ++j) {
-        if (!act[j]) continue;
-        const uint32_t b = lo[j];
-        if (rb[j] != 0 && rb[j] < r) continue;
-        if ((ra[j] == r && a[j] < e) || (rb[j] == r && b < e)) continue;  // owned by a smaller id
-        if (ra[j] != r) {
-            const uint32_t old = atomicSub(&P.sup[a[j]], 1u);
-            if (old == km2) push_edge(P, a[j], r + 1);
+        bool qa = false, qb = false;
+        uint32_t b = 0;
+        if (act[j]) {
+            b = lo[j];
+            const uint32_t rb = P.rnd[b];
+            if ((rb == 0 || rb >= r) && !((ra[j] == r && a[j] < e) || (rb == r && b < e))) {
+                if (ra[j] != r) qa = atomicSub(&P.sup[a[j]], 1u) == km2;
+                if (rb != r) qb = atomicSub(&P.sup[b], 1u) == km2;
+            }
         }
-        if (rb[j] != r) {
-            const uint32_t old = atomicSub(&P.sup[b], 1u);
-            if (old == km2) push_edge(P, b, r + 1);
-        }
+        push_edges(P, a[j], qa, r + 1);
+        push_edges(P, b, qb, r + 1);
     }
 }
 
@@ -261,8 +272,10 @@ __device__ void compact_rows(const PeelParams& P, uint32_t r_done, uint32_t* war
 // (removed edges hold kDead and never qualify).
 __device__ __forceinline__ void collect(const PeelParams& P, uint32_t thr, uint32_t rr, uint64_t tid,
                                         uint64_t nthreads) {
-    for (uint64_t j = tid; j < P.m; j += nthreads)
-        if (P.sup[j] <= thr) push_edge(P, (uint32_t)j, rr);
+    for (uint64_t j0 = tid - lane_id(); j0 < P.m; j0 += nthreads) {
+        const uint64_t j = j0 + lane_id();
+        push_edges(P, (uint32_t)j, j < P.m && P.sup[j] <= thr, rr);
+    }
 }
 
 __global__ void __launch_bounds__(kPeelThreads, 1) k_peel(PeelParams P) {
@@ -320,13 +333,14 @@ __global__ void __launch_bounds__(kPeelThreads, 1) k_peel(PeelParams P) {
             }
             // stream the whole support array (coalesced; removed edges hold kDead)
             uint32_t n_alive = 0, mn = kDead;
-            for (uint64_t j = tid; j < P.m; j += nthreads) {
-                const uint32_t s = P.sup[j];
+            for (uint64_t j0 = tid - lane; j0 < P.m; j0 += nthreads) {
+                const uint64_t j = j0 + lane;
+                const uint32_t s = j < P.m ? P.sup[j] : kDead;
                 if (s != kDead) {
                     ++n_alive;
                     mn = s < mn ? s : mn;
-                    if (s <= kg - 3) push_edge(P, (uint32_t)j, rr);
                 }
+                push_edges(P, (uint32_t)j, s != kDead && s <= kg - 3, rr);
             }
             n_alive = __reduce_add_sync(kFullMask, n_alive);
             mn = __reduce_min_sync(kFullMask, mn);
@@ -388,8 +402,8 @@ __global__ void __launch_bounds__(kPeelThreads, 1) k_peel(PeelParams P) {
                         P.tr[e] = k - 1;
                         P.sup[e] = kDead;
                     }
-                    for (uint32_t t = part * 32 + lane; t < len; t += parts * 32 * kBatch)
-                        peel_entries<kBatch>(P, e, y, base, len, t, parts * 32, r, km2);
+                    for (uint32_t t0 = part * 32; t0 < len; t0 += parts * 32 * kBatch)
+                        peel_entries<kBatch>(P, e, y, base, len, t0, parts * 32, r, km2);
                 }
             }
             // long rows: one block per slot, or several blocks per slot when slots are few
@@ -406,8 +420,9 @@ __global__ void __launch_bounds__(kPeelThreads, 1) k_peel(PeelParams P) {
                         P.tr[e] = k - 1;
                         P.sup[e] = kDead;
                     }
-                    for (uint32_t t = part * blockDim.x + threadIdx.x; t < len; t += parts * blockDim.x * kBatch)
-                        peel_entries<kBatch>(P, e, y, base, len, t, parts * blockDim.x, r, km2);
+                    const uint32_t wofs = threadIdx.x & ~31u;
+                    for (uint32_t t0 = part * blockDim.x + wofs; t0 < len; t0 += parts * blockDim.x * kBatch)
+                        peel_entries<kBatch>(P, e, y, base, len, t0, parts * blockDim.x, r, km2);
                 }
             }
             if (!grid_barrier(ctrl, nblocks, P.timeout_ns)) return;
