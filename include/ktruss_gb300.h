@@ -197,6 +197,11 @@ int kt_engine_ktruss(kt_engine* engine, const uint32_t* d_src, const uint32_t* d
 /* Synchronizes the engine stream and fills *stats.  Returns KT_ERR_TIMEOUT if the last peel
  * kernel gave up on a grid barrier. */
 int kt_engine_stats(kt_engine* engine, kt_stats* stats);
+/* Per-round log of the last decomposition or single-k call: for each of the first `cap`
+ * peel rounds, the frontier size, the level k and the device time in nanoseconds (any
+ * pointer may be NULL).  *num_rounds receives the number of rounds run. */
+int kt_engine_round_log(kt_engine* engine, uint32_t* size, uint32_t* level, uint32_t* ns, uint32_t cap,
+                        uint32_t* num_rounds);
 /* Self-test of the bounded device waits: launches a grid barrier that one block never reaches,
  * with a wait limit of timeout_ns (at most 5 s).  Returns KT_ERR_TIMEOUT when the wait expired
  * and the kernel returned as designed; the engine stays usable afterwards. */

@@ -78,6 +78,7 @@ size_t carve(kt_engine* e, char* base, uint32_t n, uint64_t N) {
     e->cap_rounds = (uint32_t)std::min<uint64_t>(m + 2, 1u << 22);
     e->round_size = c.take<uint32_t>(e->cap_rounds);
     e->round_level = c.take<uint32_t>(e->cap_rounds);
+    e->round_ns = c.take<uint32_t>(e->cap_rounds);
     e->hist = c.take<uint32_t>(hist_words);
     e->hist_words = hist_words;
     e->scan_tmp = c.take<uint32_t>(scan_words);
@@ -298,6 +299,25 @@ int kt_engine_selftest_barrier_timeout(kt_engine* e, uint64_t timeout_ns) {
     if (rc) return rc;
     e->stats_ready = true;  // the probe leaves no peel statistics behind
     return kt::barrier_timeout_probe(e, timeout_ns);
+}
+
+int kt_engine_round_log(kt_engine* e, uint32_t* size, uint32_t* level, uint32_t* ns, uint32_t cap,
+                        uint32_t* num_rounds) {
+    if (!e || !num_rounds) return fail(KT_ERR_INVALID_ARG, "kt_engine_round_log: null argument");
+    int rc = check_cuda(cudaStreamSynchronize(e->stream), "synchronize");
+    if (rc) return rc;
+    if ((rc = kt::finish_stats(e))) return rc;
+    const uint32_t R = e->stats.num_rounds;
+    *num_rounds = R;
+    const uint32_t c = std::min<uint32_t>(std::min<uint32_t>(cap, R), e->cap_rounds > 0 ? e->cap_rounds - 1 : 0);
+    if (c == 0) return KT_OK;
+    uint32_t* dst[3] = {size, level, ns};
+    uint32_t* src[3] = {e->round_size, e->round_level, e->round_ns};
+    for (int i = 0; i < 3; ++i)
+        if (dst[i] && (rc = check_cuda(cudaMemcpy(dst[i], src[i] + 1, sizeof(uint32_t) * c, cudaMemcpyDeviceToHost),
+                                       "read round log")))
+            return rc;
+    return KT_OK;
 }
 
 int kt_engine_stats(kt_engine* e, kt_stats* stats) {

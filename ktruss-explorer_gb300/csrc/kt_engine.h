@@ -65,6 +65,7 @@ struct kt_engine {
     // Per-round log: frontier size and level of each peel round.
     uint32_t* round_size = nullptr;
     uint32_t* round_level = nullptr;
+    uint32_t* round_ns = nullptr;
     uint32_t cap_rounds = 0;
     // Staging for the host-buffer entry points.
     uint32_t* in_src = nullptr;

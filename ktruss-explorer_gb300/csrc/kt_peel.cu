@@ -77,6 +77,7 @@ struct PeelParams {
     uint32_t* ctrl;
     uint32_t* round_size;
     uint32_t* round_level;
+    uint32_t* round_ns;  // device time of each round (first block's view, barrier to barrier)
     uint32_t cap_rounds;
     uint32_t n, m, big_row;
     uint32_t single_k;  // 0: full decomposition; >= 3: the k of a single-k truss
@@ -426,6 +427,7 @@ __global__ void __launch_bounds__(kPeelThreads, 1) k_peel(PeelParams P) {
                 }
             }
             if (!grid_barrier(ctrl, nblocks, P.timeout_ns)) return;
+            if (leader && rounds < P.cap_rounds) P.round_ns[rounds] = (uint32_t)(global_ns() - t_last);
             KT_PHASE(5)
             live -= S + B;
             S = ld_acquire(ctrl + kPNext + ((r + 1) & 3));
@@ -513,6 +515,7 @@ int launch_peel(kt_engine* e, uint32_t single_k) {
     P.ctrl = e->ctrl;
     P.round_size = e->round_size;
     P.round_level = e->round_level;
+    P.round_ns = e->round_ns;
     P.cap_rounds = e->cap_rounds;
     P.n = e->n;
     P.m = e->m;

@@ -114,6 +114,7 @@ def lib() -> ctypes.CDLL:
                                        ctypes.c_int]
         L.kt_engine_stats.argtypes = [_VP, ctypes.POINTER(Stats)]
         L.kt_engine_selftest_barrier_timeout.argtypes = [_VP, ctypes.c_uint64]
+        L.kt_engine_round_log.argtypes = [_VP, _U32P, _U32P, _U32P, ctypes.c_uint32, _U32P]
         for g in ("kt_gen_rmat",):
             getattr(L, g).argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_double, ctypes.c_double,
                                       ctypes.c_double, ctypes.c_uint64, ctypes.POINTER(_Edges)]
@@ -327,6 +328,15 @@ class Engine:
     def selftest_barrier_timeout(self, timeout_ns: int) -> int:
         """Status of a grid barrier that cannot complete (KT_ERR_TIMEOUT = 11 when correct)."""
         return lib().kt_engine_selftest_barrier_timeout(self._h, timeout_ns)
+
+    def round_log(self, cap: int = 1 << 20) -> dict:
+        """Frontier size, level and device nanoseconds of each peel round of the last call."""
+        size, level, ns = (np.zeros(cap, np.uint32) for _ in range(3))
+        R = ctypes.c_uint32(0)
+        _check(lib().kt_engine_round_log(self._h, size.ctypes.data_as(_U32P), level.ctypes.data_as(_U32P),
+                                         ns.ctypes.data_as(_U32P), cap, ctypes.byref(R)))
+        c = min(cap, R.value)
+        return {"size": size[:c], "level": level[:c], "ns": ns[:c], "rounds": R.value}
 
     def stats(self) -> Stats:
         s = Stats()
