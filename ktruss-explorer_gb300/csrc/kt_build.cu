@@ -15,7 +15,6 @@
 //   s_ptr[n+1], s_len[n], s_split[n]   symmetric rows (lower ranks, then higher ranks)
 //   s_col[2m], s_eid[2m]               neighbour rank and edge id per symmetric entry
 //   o_ptr[n+1], o_col[m], e_src[m]     oriented CSR/COO; edge id = index
-//   table[2^ceil(log2 2m)] (16 B)      edge hash table (lower rank, higher rank) -> edge id
 //   sorted_entry[2m]                   input entry index of each symmetric entry
 
 #include "kt_device.cuh"
@@ -151,26 +150,6 @@ __global__ void k_in_eid(const uint64_t* __restrict__ keys, uint64_t entries, un
     }
     err = __reduce_or_sync(kFullMask, err);
     if (err && lane_id() == 0) atomicOr(&ctrl[kCtrlError], err);
-}
-
-// Inserts every oriented edge (u, v) -> id into the hash table (64-bit CAS on the key half of
-// the slot, then the id).  The table is at least twice the edge count, so every insert ends.
-__global__ void k_hash_insert(const uint32_t* __restrict__ e_src, const uint32_t* __restrict__ o_col, uint32_t m,
-                              uint4* __restrict__ table, uint32_t mask) {
-    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= m) return;
-    const uint32_t lo = e_src[j], hi = o_col[j];
-    const unsigned long long key = ((unsigned long long)hi << 32) | lo;
-    uint32_t h = edge_hash(lo, hi) & mask;
-    for (uint32_t probes = 0; probes <= mask; ++probes) {
-        unsigned long long* k = reinterpret_cast<unsigned long long*>(table + h);
-        const unsigned long long prev = atomicCAS(k, ~0ull, key);
-        if (prev == ~0ull) {
-            table[h].z = j;
-            return;
-        }
-        h = (h + 1) & mask;
-    }
 }
 
 // Edge id of each input entry, kept apart from s_eid because peeling compacts the rows.
@@ -312,18 +291,6 @@ int build_graph(kt_engine* e, const uint32_t* d_src, const uint32_t* d_dst, uint
         k_entry_eid<<<grid_for(entries), kThreads, 0, st>>>(e->sorted_entry, e->s_eid, entries, e->entry_eid);
         count_launch(e);
         if ((rc = check_launch(e, "k_entry_eid"))) return rc;
-    }
-    // edge hash table over the oriented edges
-    {
-        uint64_t slots = 1024;
-        while (slots < 2 * (uint64_t)e->m) slots <<= 1;
-        e->table_mask = (uint32_t)(slots - 1);
-        if ((rc = check_cuda(cudaMemsetAsync(e->table, 0xff, slots * sizeof(uint4), st), "clear hash table"))) return rc;
-        if (e->m) {
-            k_hash_insert<<<grid_for(e->m), kThreads, 0, st>>>(e->e_src, e->o_col, e->m, e->table, e->table_mask);
-            count_launch(e);
-            if ((rc = check_launch(e, "k_hash_insert"))) return rc;
-        }
     }
     k_find_big_row<<<1, 1, 0, st>>>(e->s_ptr, n, kBigRow, e->ctrl);
     count_launch(e);

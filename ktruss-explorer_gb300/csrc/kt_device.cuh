@@ -81,35 +81,6 @@ __device__ __forceinline__ uint32_t lower_bound_u32(const uint32_t* __restrict__
 
 inline uint32_t ceil_div(uint64_t a, uint64_t b) { return (uint32_t)((a + b - 1) / b); }
 
-// ---- edge hash table -------------------------------------------------------------------------
-// Open addressing with linear probing over 16-byte slots {lo, hi, eid, 0}: lo < hi are the ranks
-// of an edge's endpoints, eid its id; lo = kHashEmpty marks a free slot.  The table has a
-// power-of-two size of at least twice the edge count, so probe runs are short.
-constexpr uint32_t kHashEmpty = 0xffffffffu;
-constexpr uint32_t kNoEdge = 0xffffffffu;
-
-__host__ __device__ __forceinline__ uint32_t edge_hash(uint32_t lo, uint32_t hi) {
-    uint64_t z = ((uint64_t)hi << 32) | lo;
-    z ^= z >> 33;
-    z *= 0xff51afd7ed558ccdull;
-    z ^= z >> 33;
-    z *= 0xc4ceb9fe1a85ec53ull;
-    z ^= z >> 33;
-    return (uint32_t)z;
-}
-
-// Edge id of (lo, hi), lo < hi, or kNoEdge.  The table is read-only while it is searched.
-__device__ __forceinline__ uint32_t hash_find(const uint4* __restrict__ table, uint32_t mask, uint32_t lo, uint32_t hi) {
-    uint32_t h = edge_hash(lo, hi) & mask;
-    for (uint32_t probes = 0; probes <= mask; ++probes) {
-        const uint4 slot = __ldg(table + h);
-        if (slot.x == lo && slot.y == hi) return slot.z;
-        if (slot.x == kHashEmpty) return kNoEdge;
-        h = (h + 1) & mask;
-    }
-    return kNoEdge;
-}
-
 __device__ __forceinline__ uint32_t ld_acquire(const uint32_t* p) {
     uint32_t v;
     asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");

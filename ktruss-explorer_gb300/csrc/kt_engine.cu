@@ -64,9 +64,6 @@ size_t carve(kt_engine* e, char* base, uint32_t n, uint64_t N) {
     e->s_eid = c.take<uint32_t>(N);
     e->o_col = c.take<uint32_t>(m);
     e->e_src = c.take<uint32_t>(m);
-    uint64_t slots = 1024;
-    while (slots < 2 * m) slots <<= 1;
-    e->table = c.take<uint4>(slots);
     e->sup = c.take<uint32_t>(m);
     e->rnd = c.take<uint32_t>(m);
     e->tr = c.take<uint32_t>(m);

@@ -41,8 +41,6 @@ struct kt_engine {
     // Per edge (m); edge id = position in the oriented CSR.
     uint32_t* o_col = nullptr;    // higher-rank endpoint
     uint32_t* e_src = nullptr;    // lower-rank endpoint
-    uint4* table = nullptr;       // edge hash table: (lo, hi) -> edge id
-    uint32_t table_mask = 0;      // slots - 1 for the current graph
     uint32_t* sup = nullptr;      // support (alive triangles)
     uint32_t* rnd = nullptr;      // 0 while alive, else the peel round that removed it
     uint32_t* tr = nullptr;       // truss number (written at removal)

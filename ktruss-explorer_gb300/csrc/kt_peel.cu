@@ -66,8 +66,6 @@ struct PeelParams {
     const uint32_t* __restrict__ o_col;
     const uint32_t* __restrict__ e_src;
     const uint32_t* __restrict__ s_ptr;
-    const uint4* __restrict__ table;
-    uint32_t table_mask;
     uint32_t* s_len;
     uint32_t* s_col;
     uint32_t* s_eid;
@@ -117,8 +115,8 @@ __device__ __forceinline__ void push_edges(const PeelParams& P, uint32_t e, bool
 // Entries of a removed edge e's shorter row (vertex x): called by all 32 lanes of a warp
 // together; lane l handles positions base + t0 + l + j*step (j < NB) that are below base + len,
 // so that the memory chains of different entries overlap.  For a neighbour w of x, edge (x,w) is
-// s_eid at the entry and edge (y,w) is looked up in the edge hash table (one 16-byte probe in
-// the common case, where a binary search in an oriented row costs several dependent loads).  Edge states during round r:
+// s_eid at the entry and edge (y,w) is found by a binary search in an oriented row (w in N+(y)
+// if w > y, else y in N+(w)); the NB searches advance in lockstep.  Edge states during round r:
 // rnd 0 = alive, r+1 = alive but queued for the next round, r = removed in this round,
 // 1..r-1 = removed earlier.  A triangle is skipped if one of its edges was removed earlier or if
 // a smaller-id edge of this round owns it; otherwise each surviving edge loses one support, and
@@ -127,31 +125,68 @@ template <int NB>
 __device__ __forceinline__ void peel_entries(const PeelParams& P, uint32_t e, uint32_t y, uint32_t base, uint32_t len,
                                              uint32_t t0, uint32_t step, uint32_t r, uint32_t km2) {
     const uint32_t lane = lane_id();
+    uint32_t a[NB], lo[NB], n[NB], end[NB], tgt[NB];
+    bool act[NB];
 #pragma unroll
     for (int j = 0; j < NB; ++j) {
         const uint32_t t = t0 + lane + (uint32_t)j * step;
-        bool act = t < len;
-        uint32_t w = y, a = 0, b = 0;
-        if (act) {
+        act[j] = t < len;
+        uint32_t w = y;
+        if (act[j]) {
             w = P.s_col[base + t];
-            a = P.s_eid[base + t];
+            a[j] = P.s_eid[base + t];
         }
-        act = act && w != y;
-        uint32_t ra = 0, rb = 0;
-        if (act) {
-            ra = P.rnd[a];
-            b = hash_find(P.table, P.table_mask, w < y ? w : y, w < y ? y : w);
-            act = b != kNoEdge && (ra == 0 || ra >= r);  // (x,w) removed earlier: triangle gone
+        act[j] = act[j] && w != y;
+        if (act[j]) {
+            const uint32_t row = w > y ? y : w;
+            tgt[j] = w > y ? w : y;
+            lo[j] = P.o_ptr[row];
+            end[j] = P.o_ptr[row + 1];
+            n[j] = end[j] - lo[j];
         }
+    }
+    uint32_t ra[NB];
+#pragma unroll
+    for (int j = 0; j < NB; ++j) {
+        if (act[j]) {
+            ra[j] = P.rnd[a[j]];
+            if (ra[j] != 0 && ra[j] < r) act[j] = false;  // (x,w) removed earlier: triangle gone
+        }
+        if (!act[j]) n[j] = 0;
+    }
+    // lockstep lower bounds
+    bool more = true;
+    while (more) {
+        more = false;
+#pragma unroll
+        for (int j = 0; j < NB; ++j) {
+            if (n[j] > 0) {
+                const uint32_t half = n[j] >> 1;
+                if (__ldg(P.o_col + lo[j] + half) < tgt[j]) {
+                    lo[j] += half + 1;
+                    n[j] -= half + 1;
+                } else {
+                    n[j] = half;
+                }
+                more = more || n[j] > 0;
+            }
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < NB; ++j) {
+        // lo is the lower bound: the edge exists only if it is inside the row and matches
+        if (act[j]) act[j] = lo[j] < end[j] && __ldg(P.o_col + lo[j]) == tgt[j];
         bool qa = false, qb = false;
-        if (act) {
-            rb = P.rnd[b];
-            if ((rb == 0 || rb >= r) && !((ra == r && a < e) || (rb == r && b < e))) {
-                if (ra != r) qa = atomicSub(&P.sup[a], 1u) == km2;
+        uint32_t b = 0;
+        if (act[j]) {
+            b = lo[j];
+            const uint32_t rb = P.rnd[b];
+            if ((rb == 0 || rb >= r) && !((ra[j] == r && a[j] < e) || (rb == r && b < e))) {
+                if (ra[j] != r) qa = atomicSub(&P.sup[a[j]], 1u) == km2;
                 if (rb != r) qb = atomicSub(&P.sup[b], 1u) == km2;
             }
         }
-        push_edges(P, a, qa, r + 1);
+        push_edges(P, a[j], qa, r + 1);
         push_edges(P, b, qb, r + 1);
     }
 }
@@ -467,8 +502,6 @@ int launch_peel(kt_engine* e, uint32_t single_k) {
     P.o_col = e->o_col;
     P.e_src = e->e_src;
     P.s_ptr = e->s_ptr;
-    P.table = e->table;
-    P.table_mask = e->table_mask;
     P.s_len = e->s_len;
     P.s_col = e->s_col;
     P.s_eid = e->s_eid;
