@@ -53,6 +53,7 @@ enum : uint32_t {
     kPCompactions = 44,
     kPPhaseNs = 48,    // [6] u64 nanoseconds per phase kind (init, level scan, collect,
                        //     compaction, mark, process), measured by block 0 barrier to barrier
+    kPEdges = 60,      // [4] edges queued for the round (chunked or long-row)
     kCtrlWords = 64,
 };
 

@@ -71,6 +71,9 @@ size_t carve(kt_engine* e, char* base, uint32_t n, uint64_t N) {
     e->q1 = c.take<uint32_t>(m);
     e->alive0 = c.take<uint32_t>(m);
     e->alive1 = c.take<uint32_t>(m);
+    e->cap_chunks = (uint32_t)std::min<uint64_t>(m + 4096, 0xfffff000u);
+    e->chunks0 = c.take<uint4>(e->cap_chunks);
+    e->chunks1 = c.take<uint4>(e->cap_chunks);
     e->fy = c.take<uint32_t>(m);
     e->fbase = c.take<uint32_t>(m);
     e->flen = c.take<uint32_t>(m);

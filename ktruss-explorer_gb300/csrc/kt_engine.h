@@ -49,6 +49,9 @@ struct kt_engine {
     uint32_t* alive0 = nullptr;   // compacted lists of alive edge ids
     uint32_t* alive1 = nullptr;
     // Per frontier slot: other endpoint, start and length of the shorter row; long-row slots.
+    uint4* chunks0 = nullptr;     // peel work chunks, by round parity
+    uint4* chunks1 = nullptr;
+    uint32_t cap_chunks = 0;
     uint32_t* fy = nullptr;
     uint32_t* fbase = nullptr;
     uint32_t* flen = nullptr;

@@ -17,17 +17,17 @@
 // support array that also finds the minimum support, so empty levels are skipped (k jumps to
 // min+3).
 //
-// One round is one phase followed by one grid barrier: warps walk the frontier edges' short
-// rows (one edge per warp, or several warps per edge when the frontier is small), then whole
-// blocks walk the long rows; per neighbour w of the shorter row's vertex x, the edge (y,w) is
-// found by a binary search in an oriented row.  An edge is stamped with the next round number
-// when its support falls below the threshold, and filed in the next round's short- or
-// long-row queue, so no separate marking phase is needed.  A removed edge's support is set to
+// One round is one phase followed by one grid barrier.  When an edge is queued (its support
+// fell below the threshold, or it is in a level's first frontier) it is stamped with the next
+// round number and the walk of its shorter row is split into chunks of up to 32 entries; in
+// the round every warp takes chunks, so a long row is spread over many warps and no warp walks
+// more than its share.  Per neighbour w of the shorter row's vertex x, the edge (y,w) is found
+// by a binary search in an oriented row.  A removed edge's support is set to
 // kDead, so a level's scan of the alive list reads one array; that scan also collects the
 // frontier of level k_last+1, and only when that level turns out to be empty does a second
 // pass collect the frontier of the next non-empty level.
-// Symmetric rows are compacted in place once the alive edges have halved since the last
-// compaction, so the walks see few removed entries.
+// Symmetric rows are compacted in place at a level start once enough edges have been removed
+// since the last compaction, so the walks see few removed entries.
 //
 // Every grid barrier wait is bounded (kPeelTimeoutNs); on expiry the kernel reports
 // KT_ERR_TIMEOUT through the control block and returns.
@@ -49,7 +49,6 @@ constexpr int kThreads = 256;          // helper kernels
 #define KT_PEEL_BATCH 1
 #endif
 constexpr int kPeelThreads = KT_PEEL_THREADS;  // persistent kernel: one block per SM
-constexpr uint32_t kLongRow = 256;     // rows longer than this are walked by a whole block
 constexpr int kBatch = KT_PEEL_BATCH;  // row entries in flight per thread
 // Rows are compacted once the alive edges fall below this fraction (num/den) of the count at
 // the last compaction.
@@ -72,8 +71,9 @@ struct PeelParams {
     uint32_t* sup;
     uint32_t* rnd;
     uint32_t* tr;
-    uint32_t* q[2];    // frontier slots with short rows, by round parity
-    uint32_t* big[2];  // frontier slots with long rows, by round parity
+    uint4* ch[2];      // work chunks of the round's frontier, by round parity
+    uint32_t cap_chunks;
+    uint32_t* big[2];  // frontier edges walked by whole blocks (chunk buffer full), by parity
     uint32_t* ctrl;
     uint32_t* round_size;
     uint32_t* round_level;
@@ -86,29 +86,60 @@ struct PeelParams {
 
 constexpr uint32_t kDead = 0xffffffffu;  // support of a removed edge
 
-// Queues edge e for round rr if `take`: stamps it and files it by the length of its shorter row
-// (a scheduling hint; the row is measured again when the round runs).  Called by all 32 lanes
-// of a warp together; the queue slots are claimed with one atomic per queue per warp.
+constexpr uint32_t kFirstChunk = 0x80000000u;
+constexpr uint32_t kNullChunk = 0xffffffffu;
+
+// Queues edge e for round rr if `take`: stamps it, and splits the walk of its shorter row into
+// chunks of up to 32 entries, one warp each, described by {edge, other endpoint y, row position,
+// entry count | kFirstChunk on the edge's first chunk}.  Rows are only compacted at level
+// starts, so the row measured here is the row walked.  Called by all 32 lanes of a warp
+// together: chunk slots are claimed with one atomic per warp.  If the chunk buffer is full, the
+// claimed slots are nulled and the edges go to the block-walked queue instead.
 __device__ __forceinline__ void push_edges(const PeelParams& P, uint32_t e, bool take, uint32_t rr) {
-    bool big = false;
+    const uint32_t mt = __ballot_sync(kFullMask, take);
+    if (!mt) return;
+    uint32_t nch = 0, y = 0, base = 0, len = 0;
     if (take) {
         P.rnd[e] = rr;
-        const uint32_t lu = P.s_len[P.e_src[e]], lv = P.s_len[P.o_col[e]];
-        big = (lu < lv ? lu : lv) > kLongRow;
+        const uint32_t u = P.e_src[e], v = P.o_col[e];
+        const uint32_t lu = P.s_len[u], lv = P.s_len[v];
+        const bool ux = lu <= lv;
+        y = ux ? v : u;
+        base = P.s_ptr[ux ? u : v];
+        len = ux ? lu : lv;
+        nch = len ? (len + 31) >> 5 : 1;
     }
-    const uint32_t ms = __ballot_sync(kFullMask, take && !big), mb = __ballot_sync(kFullMask, take && big);
-    if (!(ms | mb)) return;
     const uint32_t lane = lane_id(), slot = rr & 3;
-    uint32_t bs = 0, bb = 0;
-    if (lane == 0) {
-        if (ms) bs = atomicAdd(P.ctrl + kPNext + slot, __popc(ms));
-        if (mb) bb = atomicAdd(P.ctrl + kPBigCount + slot, __popc(mb));
+    uint32_t incl = nch;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(kFullMask, incl, o);
+        if (lane >= (uint32_t)o) incl += t;
     }
-    bs = __shfl_sync(kFullMask, bs, 0);
-    bb = __shfl_sync(kFullMask, bb, 0);
-    if (take) {
-        if (big) P.big[rr & 1][bb + __popc(mb & lanemask_lt())] = e;
-        else P.q[rr & 1][bs + __popc(ms & lanemask_lt())] = e;
+    const uint32_t total = __shfl_sync(kFullMask, incl, 31);
+    uint32_t cb = 0;
+    if (lane == 0) {
+        cb = atomicAdd(P.ctrl + kPNext + slot, total);
+        atomicAdd(P.ctrl + kPEdges + slot, __popc(mt));
+    }
+    cb = __shfl_sync(kFullMask, cb, 0);
+    uint4* ch = P.ch[rr & 1];
+    if ((uint64_t)cb + total <= P.cap_chunks) {
+        if (take) {
+            const uint32_t c0 = cb + incl - nch;
+            for (uint32_t c = 0; c < nch; ++c) {
+                const uint32_t off = c << 5;
+                const uint32_t cnt = len > off ? min(32u, len - off) : 0u;
+                ch[c0 + c] = make_uint4(e, y, base + off, cnt | (c == 0 ? kFirstChunk : 0u));
+            }
+        }
+    } else {
+        const uint64_t stop = (uint64_t)cb + total < P.cap_chunks ? (uint64_t)cb + total : P.cap_chunks;
+        for (uint64_t i = (uint64_t)cb + lane; i < stop; i += 32) ch[i] = make_uint4(kNullChunk, 0, 0, 0);
+        uint32_t bb = 0;
+        if (lane == 0) bb = atomicAdd(P.ctrl + kPBigCount + slot, __popc(mt));
+        bb = __shfl_sync(kFullMask, bb, 0);
+        if (take) P.big[rr & 1][bb + __popc(mt & lanemask_lt())] = e;
     }
 }
 
@@ -290,15 +321,19 @@ __global__ void __launch_bounds__(kPeelThreads, 1) k_peel(PeelParams P) {
     const uint32_t nwarps = (uint32_t)(nthreads >> 5);
     const bool leader = blockIdx.x == 0 && threadIdx.x == 0;
 
-    // phase clock (block 0, thread 0): time from the previous barrier to the end of this one
-    uint64_t phase_ns[6] = {0, 0, 0, 0, 0, 0};
-    uint64_t t_last = leader ? global_ns() : 0;
+    // phase clock (block 0, thread 0): time from the previous barrier to the end of this one,
+    // kept in shared memory so that it costs the other threads no registers
+    __shared__ unsigned long long phase_ns[7];  // [6] = time of the last phase boundary
+    if (leader) {
+        for (int i = 0; i < 6; ++i) phase_ns[i] = 0;
+        phase_ns[6] = global_ns();
+    }
     uint32_t compactions = 0;
 #define KT_PHASE(kind)                                   \
     if (leader) {                                        \
-        const uint64_t now_ = global_ns();               \
-        phase_ns[kind] += now_ - t_last;                 \
-        t_last = now_;                                   \
+        const unsigned long long now_ = global_ns();     \
+        phase_ns[kind] += now_ - phase_ns[6];            \
+        phase_ns[6] = now_;                              \
     }
 
     for (uint64_t j = tid; j < P.m; j += nthreads) {
@@ -322,7 +357,15 @@ __global__ void __launch_bounds__(kPeelThreads, 1) k_peel(PeelParams P) {
             if (leader) atomicOr(ctrl + kCtrlError, kErrRunaway);
             return;
         }
-        if (leader) ctrl[kPNext + ((rr + 1) & 3)] = ctrl[kPBigCount + ((rr + 1) & 3)] = 0;
+        if (leader) ctrl[kPNext + ((rr + 1) & 3)] = ctrl[kPBigCount + ((rr + 1) & 3)] = ctrl[kPEdges + ((rr + 1) & 3)] = 0;
+        // compact the rows once the alive edges have dropped enough since the last compaction
+        if (live * kCompactDen < live_at_compaction * kCompactNum) {
+            compact_rows(P, r, warp_cnt);
+            if (!grid_barrier(ctrl, nblocks, P.timeout_ns)) return;
+            KT_PHASE(3)
+            ++compactions;
+            live_at_compaction = live;
+        }
         if (P.single_k == 0) {
             // one pass over the alive list: compact it, minimum support, and the frontier of
             // level k_last+1 (the usual next level); a second pass only if that level is empty
@@ -365,15 +408,9 @@ __global__ void __launch_bounds__(kPeelThreads, 1) k_peel(PeelParams P) {
             KT_PHASE(2)
         }
         const uint32_t km2 = k - 2;
-        uint32_t S = ld_acquire(ctrl + kPNext + (rr & 3)), B = ld_acquire(ctrl + kPBigCount + (rr & 3));
-        while (S + B) {
-            if (live * kCompactDen < live_at_compaction * kCompactNum) {
-                compact_rows(P, r, warp_cnt);
-                if (!grid_barrier(ctrl, nblocks, P.timeout_ns)) return;
-                KT_PHASE(3)
-                ++compactions;
-                live_at_compaction = live;
-            }
+        uint32_t E = ld_acquire(ctrl + kPEdges + (rr & 3)), B = ld_acquire(ctrl + kPBigCount + (rr & 3));
+        uint32_t C = min(ld_acquire(ctrl + kPNext + (rr & 3)), P.cap_chunks);
+        while (E) {
             ++r;
             ++rounds;
             if (r > max_stamp) {
@@ -384,33 +421,30 @@ __global__ void __launch_bounds__(kPeelThreads, 1) k_peel(PeelParams P) {
                 const uint32_t z = (r + 2) & 3;
                 ctrl[kPNext + z] = 0;
                 ctrl[kPBigCount + z] = 0;
+                ctrl[kPEdges + z] = 0;
                 if (rounds < P.cap_rounds) {
-                    P.round_size[rounds] = S + B;
+                    P.round_size[rounds] = E;
                     P.round_level[rounds] = k;
                 }
             }
-            // short rows: one warp per slot, or several warps per slot when slots are few
+            // chunks: one warp per chunk of up to 32 row entries
             {
-                const uint32_t* q = P.q[r & 1];
-                const uint32_t parts = S >= nwarps ? 1u : min(8u, nwarps / (S ? S : 1));
-                const uint32_t units = S >= nwarps ? S : S * parts;
-                for (uint32_t u = gwarp; u < units; u += nwarps) {
-                    const uint32_t i = u % S, part = u / S;
-                    const uint32_t e = q[i];
-                    uint32_t y, base, len;
-                    slot_context(P, e, &y, &base, &len);
-                    if (part == 0 && lane == 0) {
-                        P.tr[e] = k - 1;
-                        P.sup[e] = kDead;
+                const uint4* ch = P.ch[r & 1];
+                for (uint32_t c = gwarp; c < C; c += nwarps) {
+                    const uint4 d = ch[c];
+                    if (d.x == kNullChunk) continue;
+                    if ((d.w & kFirstChunk) && lane == 0) {
+                        P.tr[d.x] = k - 1;
+                        P.sup[d.x] = kDead;
                     }
-                    for (uint32_t t0 = part * 32; t0 < len; t0 += parts * 32 * kBatch)
-                        peel_entries<kBatch>(P, e, y, base, len, t0, parts * 32, r, km2);
+                    peel_entries<1>(P, d.x, d.y, d.z, d.w & ~kFirstChunk, 0, 32, r, km2);
                 }
             }
-            // long rows: one block per slot, or several blocks per slot when slots are few
-            {
+            // edges that did not fit the chunk buffer: one block per edge, or several blocks per
+            // edge when they are few
+            if (B) {
                 const uint32_t* bq = P.big[r & 1];
-                const uint32_t parts = B >= nblocks ? 1u : nblocks / (B ? B : 1);
+                const uint32_t parts = B >= nblocks ? 1u : nblocks / B;
                 const uint32_t units = B >= nblocks ? B : B * parts;
                 for (uint32_t u = blockIdx.x; u < units; u += nblocks) {
                     const uint32_t i = u % B, part = u / B;
@@ -422,16 +456,17 @@ __global__ void __launch_bounds__(kPeelThreads, 1) k_peel(PeelParams P) {
                         P.sup[e] = kDead;
                     }
                     const uint32_t wofs = threadIdx.x & ~31u;
-                    for (uint32_t t0 = part * blockDim.x + wofs; t0 < len; t0 += parts * blockDim.x * kBatch)
-                        peel_entries<kBatch>(P, e, y, base, len, t0, parts * blockDim.x, r, km2);
+                    for (uint32_t t0 = part * blockDim.x + wofs; t0 < len; t0 += parts * blockDim.x)
+                        peel_entries<1>(P, e, y, base, len, t0, parts * blockDim.x, r, km2);
                 }
             }
             if (!grid_barrier(ctrl, nblocks, P.timeout_ns)) return;
-            if (leader && rounds < P.cap_rounds) P.round_ns[rounds] = (uint32_t)(global_ns() - t_last);
+            if (leader && rounds < P.cap_rounds) P.round_ns[rounds] = (uint32_t)(global_ns() - phase_ns[6]);
             KT_PHASE(5)
-            live -= S + B;
-            S = ld_acquire(ctrl + kPNext + ((r + 1) & 3));
+            live -= E;
+            E = ld_acquire(ctrl + kPEdges + ((r + 1) & 3));
             B = ld_acquire(ctrl + kPBigCount + ((r + 1) & 3));
+            C = min(ld_acquire(ctrl + kPNext + ((r + 1) & 3)), P.cap_chunks);
         }
         ++level;
         k_last = k;
@@ -508,10 +543,11 @@ int launch_peel(kt_engine* e, uint32_t single_k) {
     P.sup = e->sup;
     P.rnd = e->rnd;
     P.tr = e->tr;
-    P.q[0] = e->q0;
-    P.q[1] = e->q1;
-    P.big[0] = e->fy;  // the two long-row queues reuse the per-slot scratch arrays
-    P.big[1] = e->flen;
+    P.ch[0] = e->chunks0;
+    P.ch[1] = e->chunks1;
+    P.cap_chunks = e->cap_chunks;
+    P.big[0] = e->q0;
+    P.big[1] = e->q1;
     P.ctrl = e->ctrl;
     P.round_size = e->round_size;
     P.round_level = e->round_level;
