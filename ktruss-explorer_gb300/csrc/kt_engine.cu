@@ -64,7 +64,7 @@ size_t carve(kt_engine* e, char* base, uint32_t n, uint64_t N) {
     e->s_eid = c.take<uint32_t>(N);
     e->o_col = c.take<uint32_t>(m);
     e->e_src = c.take<uint32_t>(m);
-    e->sup = c.take<uint32_t>(m);
+    e->sup = c.take<uint32_t>(m + 4);  // read four at a time
     e->rnd = c.take<uint32_t>(m);
     e->tr = c.take<uint32_t>(m);
     e->q0 = c.take<uint32_t>(m);

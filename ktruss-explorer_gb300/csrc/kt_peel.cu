@@ -375,16 +375,26 @@ __global__ void __launch_bounds__(kPeelThreads, 1) k_peel(PeelParams P) {
                 ctrl[kPLAlive + z] = 0;
                 ctrl[kPLMin + z] = 0xffffffffu;
             }
-            // stream the whole support array (coalesced; removed edges hold kDead)
+            // stream the whole support array (16-byte loads, four edges per lane; removed edges
+            // hold kDead)
             uint32_t n_alive = 0, mn = kDead;
-            for (uint64_t j0 = tid - lane; j0 < P.m; j0 += nthreads) {
-                const uint64_t j = j0 + lane;
-                const uint32_t s = j < P.m ? P.sup[j] : kDead;
-                if (s != kDead) {
-                    ++n_alive;
-                    mn = s < mn ? s : mn;
+            const uint4* sup4 = reinterpret_cast<const uint4*>(P.sup);
+            const uint64_t m4 = ((uint64_t)P.m + 3) / 4;
+            for (uint64_t i0 = tid - lane; i0 < m4; i0 += nthreads) {
+                const uint64_t i = i0 + lane;
+                uint4 q4 = make_uint4(kDead, kDead, kDead, kDead);
+                if (i < m4) q4 = sup4[i];
+                const uint32_t sv[4] = {q4.x, q4.y, q4.z, q4.w};
+#pragma unroll
+                for (int c = 0; c < 4; ++c) {
+                    const uint64_t j = 4 * i + c;
+                    const uint32_t sj = j < P.m ? sv[c] : kDead;
+                    if (sj != kDead) {
+                        ++n_alive;
+                        mn = sj < mn ? sj : mn;
+                    }
+                    push_edges(P, (uint32_t)j, sj != kDead && sj <= kg - 3, rr);
                 }
-                push_edges(P, (uint32_t)j, s != kDead && s <= kg - 3, rr);
             }
             n_alive = __reduce_add_sync(kFullMask, n_alive);
             mn = __reduce_min_sync(kFullMask, mn);
