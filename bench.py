@@ -8,16 +8,19 @@ per-entry truss numbers) of the whole graph.  Prints one JSON line.
   value       edges/s = m / t_step with the COO input already in HBM (engine API, device buffers)
   e2e         edges/s through the host-buffer C ABI call kt_decompose: the pinned input entries
               are copied host->device and the per-entry truss numbers device->host every step
-  roofline    the support-count kernel: algorithmic bytes 4(n+1) + 12m per launch (row pointers,
-              column array, edge sources read once, support written once) over its CUDA-event
-              time, against the measured HBM copy bandwidth
+  roofline    the dominant kernel, the persistent peel (one launch per decomposition): algorithmic
+              bytes per launch = the bytes of the reference's full-recount schedule for the
+              passes that launch covers, sum over passes p of 4(n+1) + 12 E+_p (row pointers,
+              column array, support written and read once per pass), over the kernel's CUDA-event
+              time, against the measured HBM copy bandwidth; the support-count kernel's figure
+              (4(n+1) + 12m per launch) is reported beside it
   cpu_baseline  the reference algorithm (oracle port of its CPU path: chained count-and-prune
               passes over k) timed on a bounded sample of passes on one host core, scaled to the
               whole decomposition by the workload's exact pass volume (sum of alive edges over
               all passes of the reference schedule)
 
---impl reference times only that CPU port (the reference executable cannot be built on the
-GPU machine: its sources are not there) and prints the same line with impl "reference".
+--impl reference times only that CPU port (building the reference's own executable needs its
+sources, which this package does not ship) and prints the same line with impl "reference".
 Under torchrun, each rank decomposes its own replica (the single-graph path does not shard).
 """
 from __future__ import annotations
@@ -219,7 +222,7 @@ def run_ours(args, world, rank, local):
         td.barrier()
     torch.cuda.synchronize()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    support_ms, build_ms, peel_ms = [], [], []
+    support_ms, build_ms, peel_ms, peel_kernel_ms = [], [], [], []
     with ClockSampler(local) as clk:
         ev0.record(stream)
         for _ in range(args.steps):
@@ -228,6 +231,7 @@ def run_ours(args, world, rank, local):
             support_ms.append(s.support_ms)
             build_ms.append(s.build_ms)
             peel_ms.append(s.peel_ms)
+            peel_kernel_ms.append(s.peel_kernel_ms)
         ev1.record(stream)
         torch.cuda.synchronize()
     ms = ev0.elapsed_time(ev1) / args.steps
@@ -261,16 +265,18 @@ def run_ours(args, world, rank, local):
         raise RuntimeError("host-buffer and device-buffer decompositions differ")
 
     hbm, hbm_kind = peaks()
-    sup_ms = statistics.mean(support_ms)
-    sup_bytes = 4 * (n + 1) + 12 * m
-    achieved = sup_bytes / (sup_ms * 1e-3) / 1e9
-    traffic = None
+    traffic = {}
     try:
         with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
-            traffic = json.load(f).get(args.workload, {}).get("k_support")
+            traffic = json.load(f).get(args.workload, {})
     except Exception:
         pass
+    sup_ms = statistics.mean(support_ms)
+    sup_bytes = 4 * (n + 1) + 12 * m
+    sup_gbs = sup_bytes / (sup_ms * 1e-3) / 1e9
+    pk_ms = statistics.mean(peel_kernel_ms)
     plain_bytes = 4 * (n + 1) * st.plain_passes + 12 * st.plain_alive_sum
+    pk_gbs = plain_bytes / (pk_ms * 1e-3) / 1e9
     vol = PASS_VOLUME.get(args.workload)
     if vol and (vol["plain_passes"] != st.plain_passes or vol["plain_alive_sum"] != st.plain_alive_sum):
         raise RuntimeError(f"pass volume changed: {st.plain_passes}/{st.plain_alive_sum} vs {vol}")
@@ -286,11 +292,13 @@ def run_ours(args, world, rank, local):
             "e2e": {"value": m * world / e2e_s, "unit": "edges/s", "h2d_bytes_per_step": 8 * N,
                     "d2h_bytes_per_step": 4 * N},
             "gpu_launches": launches // args.steps * args.steps,
-            "roofline": {"bound": "hbm", "kernel": "k_support", "achieved": achieved, "peak": hbm,
-                         "peak_kind": hbm_kind, "unit": "GB/s", "frac": achieved / hbm, "traffic": traffic,
-                         "algorithmic_bytes": sup_bytes},
-            "plain_schedule": {"passes": st.plain_passes, "alive_sum": st.plain_alive_sum, "bytes": plain_bytes,
-                               "gbs": plain_bytes / (ms * 1e-3) / 1e9},
+            "roofline": {"bound": "hbm", "kernel": "k_peel", "achieved": pk_gbs, "peak": hbm,
+                         "peak_kind": hbm_kind, "unit": "GB/s", "frac": pk_gbs / hbm,
+                         "traffic": traffic.get("k_peel"), "algorithmic_bytes": plain_bytes,
+                         "kernel_ms": pk_ms, "passes": st.plain_passes, "alive_sum": st.plain_alive_sum},
+            "roofline_support": {"bound": "hbm", "kernel": "k_support", "achieved": sup_gbs, "peak": hbm,
+                                 "unit": "GB/s", "frac": sup_gbs / hbm, "traffic": traffic.get("k_support"),
+                                 "algorithmic_bytes": sup_bytes, "kernel_ms": sup_ms},
             "clocks": clk.summary()}
     if rank == 0 and world == 1 and not args.no_cpu:
         s, rate = cpu_sample(n, src, dst, args.cpu_budget, None)

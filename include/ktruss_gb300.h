@@ -173,6 +173,7 @@ typedef struct kt_stats {
     float peel_phase_ms[6];      /* peel kernel time by phase (init, level scan, frontier
                                     collection, row compaction, mark, process), barrier to
                                     barrier, as seen by its first block                        */
+    float peel_kernel_ms;        /* CUDA-event time of the peel kernel launch alone            */
 } kt_stats;
 
 /* Creates an engine on `device` with its own non-blocking CUDA stream. */

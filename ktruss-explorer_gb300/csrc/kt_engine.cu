@@ -231,6 +231,8 @@ int kt_engine_create(int device, kt_engine** out) {
         (rc = check_cuda(cudaEventCreate(&e->ev_stop), "create event")) ||
         (rc = check_cuda(cudaEventCreate(&e->ev_built), "create event")) ||
         (rc = check_cuda(cudaEventCreate(&e->ev_counted), "create event")) ||
+        (rc = check_cuda(cudaEventCreate(&e->ev_peel0), "create event")) ||
+        (rc = check_cuda(cudaEventCreate(&e->ev_peel1), "create event")) ||
         (rc = check_cuda(cudaMalloc(&e->ctrl, sizeof(uint32_t) * kt::kCtrlWords), "allocate control block")) ||
         (rc = check_cuda(cudaMallocHost(&e->h_ctrl, sizeof(uint32_t) * kt::kCtrlWords), "allocate host mirror"))) {
         kt_engine_destroy(e);
@@ -251,6 +253,8 @@ int kt_engine_destroy(kt_engine* e) {
     if (e->ev_stop) cudaEventDestroy(e->ev_stop);
     if (e->ev_built) cudaEventDestroy(e->ev_built);
     if (e->ev_counted) cudaEventDestroy(e->ev_counted);
+    if (e->ev_peel0) cudaEventDestroy(e->ev_peel0);
+    if (e->ev_peel1) cudaEventDestroy(e->ev_peel1);
     if (e->stream) cudaStreamDestroy(e->stream);
     delete e;
     return KT_OK;

@@ -13,6 +13,8 @@ struct kt_engine {
     int num_sms = 0;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev_start = nullptr, ev_stop = nullptr, ev_built = nullptr, ev_counted = nullptr;
+    cudaEvent_t ev_peel0 = nullptr, ev_peel1 = nullptr;  // around the peel kernel launch
+    bool peel_timed = false;
     uint64_t launches = 0;
 
     // Workspace arena: one allocation carved into the arrays below.

@@ -569,11 +569,14 @@ int launch_peel(kt_engine* e, uint32_t single_k) {
     P.single_k = single_k;
     P.timeout_ns = kPeelTimeoutNs;
     void* args[] = {&P};
+    if ((rc = check_cuda(cudaEventRecord(e->ev_peel0, e->stream), "record event"))) return rc;
     rc = check_cuda(cudaLaunchCooperativeKernel((const void*)k_peel, dim3((unsigned)e->num_sms), dim3(kPeelThreads),
                                                 args, 0, e->stream),
                     "cooperative launch of k_peel");
     count_launch(e);
-    return rc;
+    if (rc) return rc;
+    e->peel_timed = true;
+    return check_cuda(cudaEventRecord(e->ev_peel1, e->stream), "record event");
 }
 
 int triangles(kt_engine* e) {
@@ -592,6 +595,7 @@ int triangles(kt_engine* e) {
 
 int peel_decompose(kt_engine* e) {
     int rc;
+    e->peel_timed = false;
     e->peel_mode = 0;
     e->stats_ready = false;
     if ((rc = triangles(e))) return rc;
@@ -601,6 +605,7 @@ int peel_decompose(kt_engine* e) {
 
 int peel_single_k(kt_engine* e, uint32_t k) {
     int rc;
+    e->peel_timed = false;
     e->peel_mode = 1;
     e->stats_ready = false;
     if (k >= 3 && (rc = triangles(e))) return rc;
@@ -651,6 +656,7 @@ int finish_stats(kt_engine* e) {
     if (e->stats_ready) return KT_OK;
     if (e->m == 0 || e->peel_mode == 2) {
         e->stats.compactions = 0;
+        e->stats.peel_kernel_ms = 0;
         for (int i = 0; i < 6; ++i) e->stats.peel_phase_ms[i] = 0;
         e->stats.k_max = 0;
         e->stats.num_rounds = e->stats.num_levels = e->stats.plain_passes = 0;
@@ -671,6 +677,10 @@ int finish_stats(kt_engine* e) {
     e->stats.num_rounds = m ? e->h_ctrl[kPRounds] : 0;
     e->stats.num_levels = m ? e->h_ctrl[kPLevels] : 0;
     e->stats.compactions = e->h_ctrl[kPCompactions];
+    e->stats.peel_kernel_ms = 0;
+    if (e->peel_timed &&
+        (rc = check_cuda(cudaEventElapsedTime(&e->stats.peel_kernel_ms, e->ev_peel0, e->ev_peel1), "elapsed time")))
+        return rc;
     for (int i = 0; i < 6; ++i)
         e->stats.peel_phase_ms[i] =
             (float)(((uint64_t)e->h_ctrl[kPPhaseNs + 2 * i + 1] << 32 | e->h_ctrl[kPPhaseNs + 2 * i]) * 1e-6);

@@ -67,7 +67,8 @@ class Stats(ctypes.Structure):
                 ("plain_alive_sum", ctypes.c_uint64), ("plain_passes", ctypes.c_uint32),
                 ("kernel_launches", ctypes.c_uint64), ("last_ms", ctypes.c_float),
                 ("build_ms", ctypes.c_float), ("support_ms", ctypes.c_float), ("peel_ms", ctypes.c_float),
-                ("compactions", ctypes.c_uint32), ("peel_phase_ms", ctypes.c_float * 6)]
+                ("compactions", ctypes.c_uint32), ("peel_phase_ms", ctypes.c_float * 6),
+                ("peel_kernel_ms", ctypes.c_float)]
 
     PHASES = ("init", "level_scan", "collect", "compaction", "mark", "process")
 
