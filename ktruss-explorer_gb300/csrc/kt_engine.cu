@@ -40,9 +40,11 @@ struct Carver {
     }
 };
 
-// Lays out every array of the engine for the given capacity; with base == nullptr it only
-// measures the arena.
-size_t carve(kt_engine* e, char* base, uint32_t n, uint64_t N) {
+}  // namespace
+
+// Lays out every array of the engine for the given capacity inside `base`; with base == nullptr
+// it only measures.  `staging` adds the host-transfer buffers of the host-buffer entry points.
+size_t carve(kt_engine* e, char* base, uint32_t n, uint64_t N, bool staging) {
     const uint64_t m = N / 2 + 1;
     const uint64_t keys = std::max<uint64_t>(N, n);
     const uint64_t sort_blocks = (keys + 2047) / 2048;
@@ -69,15 +71,9 @@ size_t carve(kt_engine* e, char* base, uint32_t n, uint64_t N) {
     e->tr = c.take<uint32_t>(m);
     e->q0 = c.take<uint32_t>(m);
     e->q1 = c.take<uint32_t>(m);
-    e->alive0 = c.take<uint32_t>(m);
-    e->alive1 = c.take<uint32_t>(m);
     e->cap_chunks = (uint32_t)std::min<uint64_t>(m + 4096, 0xfffff000u);
     e->chunks0 = c.take<uint4>(e->cap_chunks);
     e->chunks1 = c.take<uint4>(e->cap_chunks);
-    e->fy = c.take<uint32_t>(m);
-    e->fbase = c.take<uint32_t>(m);
-    e->flen = c.take<uint32_t>(m);
-    e->big = c.take<uint32_t>(m);
     e->cap_rounds = (uint32_t)std::min<uint64_t>(m + 2, 1u << 22);
     e->round_size = c.take<uint32_t>(e->cap_rounds);
     e->round_level = c.take<uint32_t>(e->cap_rounds);
@@ -86,14 +82,14 @@ size_t carve(kt_engine* e, char* base, uint32_t n, uint64_t N) {
     e->hist_words = hist_words;
     e->scan_tmp = c.take<uint32_t>(scan_words);
     e->scan_tmp_words = scan_words;
-    e->in_src = c.take<uint32_t>(N);
-    e->in_dst = c.take<uint32_t>(N);
-    e->out_u32 = c.take<uint32_t>(N);
-    e->out_u8 = c.take<uint8_t>(N);
+    if (staging) {
+        e->in_src = c.take<uint32_t>(N);
+        e->in_dst = c.take<uint32_t>(N);
+        e->out_u32 = c.take<uint32_t>(N);
+        e->out_u8 = c.take<uint8_t>(N);
+    }
     return c.off;
 }
-
-}  // namespace
 
 int reserve(kt_engine* e, uint32_t max_nodes, uint64_t max_entries) {
     if (max_nodes <= e->cap_nodes && max_entries <= e->cap_entries && e->arena) return KT_OK;
@@ -107,7 +103,7 @@ int reserve(kt_engine* e, uint32_t max_nodes, uint64_t max_entries) {
         e->arena = nullptr;
         e->arena_bytes = 0;
     }
-    const size_t bytes = carve(e, nullptr, max_nodes, max_entries);
+    const size_t bytes = carve(e, nullptr, max_nodes, max_entries, true);
     void* p = nullptr;
     if ((rc = check_cuda(cudaMalloc(&p, bytes), "allocate engine workspace"))) {
         e->cap_nodes = 0;
@@ -116,7 +112,7 @@ int reserve(kt_engine* e, uint32_t max_nodes, uint64_t max_entries) {
     }
     e->arena = p;
     e->arena_bytes = bytes;
-    carve(e, static_cast<char*>(p), max_nodes, max_entries);
+    carve(e, static_cast<char*>(p), max_nodes, max_entries, true);
     e->cap_nodes = max_nodes;
     e->cap_entries = max_entries;
     return KT_OK;

@@ -46,18 +46,11 @@ struct kt_engine {
     uint32_t* sup = nullptr;      // support (alive triangles)
     uint32_t* rnd = nullptr;      // 0 while alive, else the peel round that removed it
     uint32_t* tr = nullptr;       // truss number (written at removal)
-    uint32_t* q0 = nullptr;       // frontier queues
+    uint32_t* q0 = nullptr;       // edges walked by whole blocks, by round parity
     uint32_t* q1 = nullptr;
-    uint32_t* alive0 = nullptr;   // compacted lists of alive edge ids
-    uint32_t* alive1 = nullptr;
-    // Per frontier slot: other endpoint, start and length of the shorter row; long-row slots.
     uint4* chunks0 = nullptr;     // peel work chunks, by round parity
     uint4* chunks1 = nullptr;
     uint32_t cap_chunks = 0;
-    uint32_t* fy = nullptr;
-    uint32_t* fbase = nullptr;
-    uint32_t* flen = nullptr;
-    uint32_t* big = nullptr;
     uint32_t big_row = 0;         // ranks >= big_row have rows of kBigRow entries or more
     // Scratch for scans and sort histograms.
     uint32_t* scan_tmp = nullptr;
@@ -97,6 +90,7 @@ int check_cuda(cudaError_t err, const char* what);
 int check_launch(kt_engine* e, const char* what);
 
 int reserve(kt_engine* e, uint32_t max_nodes, uint64_t max_entries);
+size_t carve(kt_engine* e, char* base, uint32_t n, uint64_t N, bool staging);
 
 // kt_sort.cu
 int exclusive_scan(kt_engine* e, const uint32_t* in, uint32_t* out, uint64_t n);

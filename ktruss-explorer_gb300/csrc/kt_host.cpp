@@ -13,19 +13,18 @@
 
 namespace kt {
 
-static thread_local std::string g_last_error;
+// Fixed-size per-thread message buffer: recording an error never touches the heap.
+static thread_local char g_last_error[1024];
 
 int fail(int code, const char* fmt, ...) {
-    char buf[1024];
     va_list ap;
     va_start(ap, fmt);
-    vsnprintf(buf, sizeof(buf), fmt, ap);
+    vsnprintf(g_last_error, sizeof(g_last_error), fmt, ap);
     va_end(ap);
-    g_last_error = buf;
     return code;
 }
 
-void clear_error() { g_last_error.clear(); }
+void clear_error() { g_last_error[0] = '\0'; }
 
 }  // namespace kt
 
@@ -33,7 +32,7 @@ using kt::fail;
 
 extern "C" {
 
-const char* kt_last_error(void) { return kt::g_last_error.c_str(); }
+const char* kt_last_error(void) { return kt::g_last_error; }
 
 const char* kt_status_string(int s) {
     switch (s) {

@@ -569,12 +569,13 @@ int launch_peel(kt_engine* e, uint32_t single_k) {
     P.single_k = single_k;
     P.timeout_ns = kPeelTimeoutNs;
     void* args[] = {&P};
-    if ((rc = check_cuda(cudaEventRecord(e->ev_peel0, e->stream), "record event"))) return rc;
+    const bool timed = e->ev_peel0 && e->ev_peel1;
+    if (timed && (rc = check_cuda(cudaEventRecord(e->ev_peel0, e->stream), "record event"))) return rc;
     rc = check_cuda(cudaLaunchCooperativeKernel((const void*)k_peel, dim3((unsigned)e->num_sms), dim3(kPeelThreads),
                                                 args, 0, e->stream),
                     "cooperative launch of k_peel");
     count_launch(e);
-    if (rc) return rc;
+    if (rc || !timed) return rc;
     e->peel_timed = true;
     return check_cuda(cudaEventRecord(e->ev_peel1, e->stream), "record event");
 }
