@@ -208,6 +208,20 @@ int kt_engine_round_log(kt_engine* engine, uint32_t* size, uint32_t* level, uint
  * and the kernel returned as designed; the engine stays usable afterwards. */
 int kt_engine_selftest_barrier_timeout(kt_engine* engine, uint64_t timeout_ns);
 
+/* Decomposition that allocates nothing (no counterpart in the reference).  For callers that
+ * cannot let a library allocate device memory: programs whose device memory is owned by one
+ * memory manager with a fixed budget, and latency-sensitive loops that cannot afford
+ * cudaMalloc/cudaFree (which may synchronize the device).  Same inputs and outputs as
+ * kt_engine_decompose on the current device and `stream` (a cudaStream_t, NULL = default stream);
+ * all scratch lives in a 40 MiB static device array held by every GPU that loads this library
+ * until the process exits.  Limits: at most 524,288 entries (262,144 undirected edges) and
+ * 131,072 vertices, else KT_ERR_TOO_LARGE.  The first call on a device sets the array up and
+ * should happen before any stream capture.  Calls on a device share the array; they are
+ * serialized and each returns after its GPU work has finished (overlapping work would race). */
+int kt_decompose_noalloc(const uint32_t* d_src, const uint32_t* d_dst, uint64_t num_entries,
+                         uint32_t num_nodes, uint32_t* d_truss_per_entry, uint32_t* d_k_max,
+                         void* stream);
+
 /* ---- seeded generators (no counterpart in the reference, which ships no data) --------- */
 int kt_gen_rmat(uint32_t scale, uint32_t edge_factor, double a, double b, double c,
                 uint64_t seed, kt_edges* out);

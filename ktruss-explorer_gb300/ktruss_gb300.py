@@ -115,6 +115,7 @@ def lib() -> ctypes.CDLL:
                                        ctypes.c_int]
         L.kt_engine_stats.argtypes = [_VP, ctypes.POINTER(Stats)]
         L.kt_engine_selftest_barrier_timeout.argtypes = [_VP, ctypes.c_uint64]
+        L.kt_decompose_noalloc.argtypes = [_VP, _VP, ctypes.c_uint64, ctypes.c_uint32, _VP, _VP, _VP]
         L.kt_engine_round_log.argtypes = [_VP, _U32P, _U32P, _U32P, ctypes.c_uint32, _U32P]
         for g in ("kt_gen_rmat",):
             getattr(L, g).argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_double, ctypes.c_double,
@@ -343,6 +344,15 @@ class Engine:
         s = Stats()
         _check(lib().kt_engine_stats(self._h, ctypes.byref(s)))
         return s
+
+
+def decompose_noalloc(d_src: int, d_dst: int, num_entries: int, num_nodes: int, d_truss: int, d_k_max: int = 0,
+                      stream: int = 0) -> None:
+    """kt_decompose_noalloc: the decomposition with device buffers, without any allocation by the
+    library (scratch in a fixed static device array; at most 524,288 entries and 131,072
+    vertices).  For callers whose device memory must not be allocated behind their back."""
+    _check(lib().kt_decompose_noalloc(d_src, d_dst, num_entries, num_nodes, d_truss, d_k_max or None,
+                                      stream or None))
 
 
 # ---- generators -----------------------------------------------------------------------------
