@@ -32,18 +32,24 @@ inline uint32_t grid_for(uint64_t n, int threads = kThreads) {
     return (uint32_t)(b == 0 ? 1 : b);
 }
 
+// Degree histogram with per-warp aggregation: lanes holding the same source add once (inputs
+// listed row by row put a hub's many entries in the same warps).
 __global__ void k_degree(const uint32_t* __restrict__ src, const uint32_t* __restrict__ dst, uint64_t entries,
                          uint32_t n, uint32_t* __restrict__ deg, uint32_t* __restrict__ ctrl) {
     uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    uint32_t err = 0;
+    uint32_t err = 0, s = 0xffffffffu;
     if (i < entries) {
-        uint32_t s = src[i], d = dst[i];
-        if (s >= n || d >= n) err = kErrBadVertex;
-        else {
-            if (s == d) err = kErrSelfLoop;
-            atomicAdd(&deg[s], 1u);
+        s = src[i];
+        const uint32_t d = dst[i];
+        if (s >= n || d >= n) {
+            err = kErrBadVertex;
+            s = 0xffffffffu;
+        } else if (s == d) {
+            err = kErrSelfLoop;
         }
     }
+    const uint32_t peers = __match_any_sync(kFullMask, s);
+    if (s != 0xffffffffu && lane_id() == (uint32_t)(__ffs(peers) - 1)) atomicAdd(&deg[s], __popc(peers));
     err = __reduce_or_sync(kFullMask, err);
     if (err && lane_id() == 0) atomicOr(&ctrl[kCtrlError], err);
 }

@@ -380,20 +380,28 @@ __global__ void __launch_bounds__(kPeelThreads, 1) k_peel(PeelParams P) {
             uint32_t n_alive = 0, mn = kDead;
             const uint4* sup4 = reinterpret_cast<const uint4*>(P.sup);
             const uint64_t m4 = ((uint64_t)P.m + 3) / 4;
-            for (uint64_t i0 = tid - lane; i0 < m4; i0 += nthreads) {
-                const uint64_t i = i0 + lane;
-                uint4 q4 = make_uint4(kDead, kDead, kDead, kDead);
-                if (i < m4) q4 = sup4[i];
-                const uint32_t sv[4] = {q4.x, q4.y, q4.z, q4.w};
+            constexpr int kScanUnroll = 2;  // 16-byte loads in flight per lane
+            for (uint64_t i0 = tid - lane; i0 < m4; i0 += nthreads * kScanUnroll) {
+                uint4 q4[kScanUnroll];
 #pragma unroll
-                for (int c = 0; c < 4; ++c) {
-                    const uint64_t j = 4 * i + c;
-                    const uint32_t sj = j < P.m ? sv[c] : kDead;
-                    if (sj != kDead) {
-                        ++n_alive;
-                        mn = sj < mn ? sj : mn;
+                for (int u = 0; u < kScanUnroll; ++u) {
+                    const uint64_t i = i0 + (uint64_t)u * nthreads + lane;
+                    q4[u] = i < m4 ? sup4[i] : make_uint4(kDead, kDead, kDead, kDead);
+                }
+#pragma unroll
+                for (int u = 0; u < kScanUnroll; ++u) {
+                    const uint64_t i = i0 + (uint64_t)u * nthreads + lane;
+                    const uint32_t sv[4] = {q4[u].x, q4[u].y, q4[u].z, q4[u].w};
+#pragma unroll
+                    for (int c = 0; c < 4; ++c) {
+                        const uint64_t j = 4 * i + c;
+                        const uint32_t sj = j < P.m ? sv[c] : kDead;
+                        if (sj != kDead) {
+                            ++n_alive;
+                            mn = sj < mn ? sj : mn;
+                        }
+                        push_edges(P, (uint32_t)j, sj != kDead && sj <= kg - 3, rr);
                     }
-                    push_edges(P, (uint32_t)j, sj != kDead && sj <= kg - 3, rr);
                 }
             }
             n_alive = __reduce_add_sync(kFullMask, n_alive);
