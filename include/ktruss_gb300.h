@@ -203,6 +203,11 @@ int kt_engine_stats(kt_engine* engine, kt_stats* stats);
  * pointer may be NULL).  *num_rounds receives the number of rounds run. */
 int kt_engine_round_log(kt_engine* engine, uint32_t* size, uint32_t* level, uint32_t* ns, uint32_t cap,
                         uint32_t* num_rounds);
+/* Per-level log of the last call: for each of the first `cap` peel levels, k, the alive edges at
+ * its start, the device time of its start (alive-edge scan and first frontier) in nanoseconds,
+ * and the size of its first frontier (any pointer may be NULL). */
+int kt_engine_level_log(kt_engine* engine, uint32_t* k, uint32_t* alive, uint32_t* ns, uint32_t* frontier,
+                        uint32_t cap, uint32_t* num_levels);
 /* Self-test of the bounded device waits: launches a grid barrier that one block never reaches,
  * with a wait limit of timeout_ns (at most 5 s).  Returns KT_ERR_TIMEOUT when the wait expired
  * and the kernel returned as designed; the engine stays usable afterwards. */

@@ -78,6 +78,10 @@ size_t carve(kt_engine* e, char* base, uint32_t n, uint64_t N, bool staging) {
     e->round_size = c.take<uint32_t>(e->cap_rounds);
     e->round_level = c.take<uint32_t>(e->cap_rounds);
     e->round_ns = c.take<uint32_t>(e->cap_rounds);
+    e->level_k = c.take<uint32_t>(e->cap_rounds);
+    e->level_alive = c.take<uint32_t>(e->cap_rounds);
+    e->level_ns = c.take<uint32_t>(e->cap_rounds);
+    e->level_front = c.take<uint32_t>(e->cap_rounds);
     e->hist = c.take<uint32_t>(hist_words);
     e->hist_words = hist_words;
     e->scan_tmp = c.take<uint32_t>(scan_words);
@@ -319,6 +323,25 @@ int kt_engine_round_log(kt_engine* e, uint32_t* size, uint32_t* level, uint32_t*
     for (int i = 0; i < 3; ++i)
         if (dst[i] && (rc = check_cuda(cudaMemcpy(dst[i], src[i] + 1, sizeof(uint32_t) * c, cudaMemcpyDeviceToHost),
                                        "read round log")))
+            return rc;
+    return KT_OK;
+}
+
+int kt_engine_level_log(kt_engine* e, uint32_t* k, uint32_t* alive, uint32_t* ns, uint32_t* frontier, uint32_t cap,
+                        uint32_t* num_levels) {
+    if (!e || !num_levels) return fail(KT_ERR_INVALID_ARG, "kt_engine_level_log: null argument");
+    int rc = check_cuda(cudaStreamSynchronize(e->stream), "synchronize");
+    if (rc) return rc;
+    if ((rc = kt::finish_stats(e))) return rc;
+    const uint32_t L = e->stats.num_levels;
+    *num_levels = L;
+    const uint32_t c = std::min<uint32_t>(std::min<uint32_t>(cap, L), e->cap_rounds);
+    if (c == 0) return KT_OK;
+    uint32_t* dst[4] = {k, alive, ns, frontier};
+    uint32_t* src[4] = {e->level_k, e->level_alive, e->level_ns, e->level_front};
+    for (int i = 0; i < 4; ++i)
+        if (dst[i] &&
+            (rc = check_cuda(cudaMemcpy(dst[i], src[i], sizeof(uint32_t) * c, cudaMemcpyDeviceToHost), "read level log")))
             return rc;
     return KT_OK;
 }

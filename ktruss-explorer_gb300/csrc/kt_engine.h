@@ -64,6 +64,10 @@ struct kt_engine {
     uint32_t* round_size = nullptr;
     uint32_t* round_level = nullptr;
     uint32_t* round_ns = nullptr;
+    uint32_t* level_k = nullptr;      // per-level log (k, alive, start time, first frontier)
+    uint32_t* level_alive = nullptr;
+    uint32_t* level_ns = nullptr;
+    uint32_t* level_front = nullptr;
     uint32_t cap_rounds = 0;
     // Staging for the host-buffer entry points.
     uint32_t* in_src = nullptr;

@@ -78,6 +78,10 @@ struct PeelParams {
     uint32_t* round_size;
     uint32_t* round_level;
     uint32_t* round_ns;  // device time of each round (first block's view, barrier to barrier)
+    uint32_t* level_k;     // per level: k, alive edges at its start, device time of its start
+    uint32_t* level_alive; //   (scan and frontier collection), first frontier size
+    uint32_t* level_ns;
+    uint32_t* level_front;
     uint32_t cap_rounds;
     uint32_t n, m, big_row;
     uint32_t single_k;  // 0: full decomposition; >= 3: the k of a single-k truss
@@ -351,6 +355,7 @@ __global__ void __launch_bounds__(kPeelThreads, 1) k_peel(PeelParams P) {
     const uint64_t max_stamp = 2ull * P.m + 8;
     for (;;) {
         const uint32_t ls = level & 3;
+        const unsigned long long level_t0 = leader ? global_ns() : 0ull;
         r += 1;                     // skipped stamp
         const uint32_t rr = r + 1;  // stamp of this level's first round
         if (level > P.m + 1 || rr > max_stamp) {
@@ -427,6 +432,12 @@ __global__ void __launch_bounds__(kPeelThreads, 1) k_peel(PeelParams P) {
         }
         const uint32_t km2 = k - 2;
         uint32_t E = ld_acquire(ctrl + kPEdges + (rr & 3)), B = ld_acquire(ctrl + kPBigCount + (rr & 3));
+        if (leader && level < P.cap_rounds) {
+            P.level_k[level] = k;
+            P.level_alive[level] = P.single_k ? P.m : ld_acquire(ctrl + kPLAlive + ls);
+            P.level_ns[level] = (uint32_t)(global_ns() - level_t0);
+            P.level_front[level] = E;
+        }
         uint32_t C = min(ld_acquire(ctrl + kPNext + (rr & 3)), P.cap_chunks);
         while (E) {
             ++r;
@@ -570,6 +581,10 @@ int launch_peel(kt_engine* e, uint32_t single_k) {
     P.round_size = e->round_size;
     P.round_level = e->round_level;
     P.round_ns = e->round_ns;
+    P.level_k = e->level_k;
+    P.level_alive = e->level_alive;
+    P.level_ns = e->level_ns;
+    P.level_front = e->level_front;
     P.cap_rounds = e->cap_rounds;
     P.n = e->n;
     P.m = e->m;

@@ -116,6 +116,7 @@ def lib() -> ctypes.CDLL:
         L.kt_engine_stats.argtypes = [_VP, ctypes.POINTER(Stats)]
         L.kt_engine_selftest_barrier_timeout.argtypes = [_VP, ctypes.c_uint64]
         L.kt_decompose_noalloc.argtypes = [_VP, _VP, ctypes.c_uint64, ctypes.c_uint32, _VP, _VP, _VP]
+        L.kt_engine_level_log.argtypes = [_VP, _U32P, _U32P, _U32P, _U32P, ctypes.c_uint32, _U32P]
         L.kt_engine_round_log.argtypes = [_VP, _U32P, _U32P, _U32P, ctypes.c_uint32, _U32P]
         for g in ("kt_gen_rmat",):
             getattr(L, g).argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_double, ctypes.c_double,
@@ -339,6 +340,14 @@ class Engine:
                                          ns.ctypes.data_as(_U32P), cap, ctypes.byref(R)))
         c = min(cap, R.value)
         return {"size": size[:c], "level": level[:c], "ns": ns[:c], "rounds": R.value}
+
+    def level_log(self, cap: int = 1 << 20) -> dict:
+        """k, alive edges, start-of-level device nanoseconds and first frontier of each level."""
+        arr = [np.zeros(cap, np.uint32) for _ in range(4)]
+        L = ctypes.c_uint32(0)
+        _check(lib().kt_engine_level_log(self._h, *[a.ctypes.data_as(_U32P) for a in arr], cap, ctypes.byref(L)))
+        c = min(cap, L.value)
+        return {"k": arr[0][:c], "alive": arr[1][:c], "ns": arr[2][:c], "frontier": arr[3][:c], "levels": L.value}
 
     def stats(self) -> Stats:
         s = Stats()
