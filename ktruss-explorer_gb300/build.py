@@ -21,6 +21,7 @@ CSRC = os.path.join(PKG, "csrc")
 OBJ = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "lib", "libktruss_gb300.so")
 CLI = os.path.join(PKG, "bin", "ktruss")
+COMPAT = os.path.join(PKG, "lib", "libktruss_compat.so")
 INCLUDE = os.path.join(ROOT, "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -31,6 +32,7 @@ CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-u
 LIB_SOURCES = ["kt_host.cpp", "kt_gen.cpp", "kt_sort.cu", "kt_build.cu", "kt_support.cu", "kt_peel.cu",
                "kt_engine.cu", "kt_noalloc.cu"]
 CLI_SOURCES = ["ktruss_cli.cpp"]
+COMPAT_SOURCES = ["ktruss_compat.cpp"]
 
 
 def _nvcc() -> str:
@@ -72,7 +74,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     os.makedirs(OBJ, exist_ok=True)
     os.makedirs(os.path.dirname(LIB), exist_ok=True)
     os.makedirs(os.path.dirname(CLI), exist_ok=True)
-    srcs = LIB_SOURCES + CLI_SOURCES
+    srcs = LIB_SOURCES + CLI_SOURCES + COMPAT_SOURCES
     with cf.ThreadPoolExecutor(max_workers=min(len(srcs), os.cpu_count() or 4)) as ex:
         objs = dict(zip(srcs, ex.map(lambda s: _compile(s, force), srcs)))
     lib_objs = [objs[s] for s in LIB_SOURCES]
@@ -92,6 +94,15 @@ def build(force: bool = False, verbose: bool = False) -> str:
             raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
         if verbose:
             print("linked", CLI)
+    compat_objs = [objs[s] for s in COMPAT_SOURCES]
+    if force or _stale(COMPAT, compat_objs + [LIB]):
+        cmd = [os.environ.get("CXX", "g++"), "-shared", "-o", COMPAT] + compat_objs + [
+            "-L", os.path.dirname(LIB), "-lktruss_gb300", "-Wl,-rpath,$ORIGIN"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+        if verbose:
+            print("linked", COMPAT)
     return LIB
 
 
