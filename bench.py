@@ -47,6 +47,14 @@ WORKLOADS = {
     "rmat16": dict(scale=16, ef=16, a=0.57, b=0.19, c=0.19, seed=1),
 }
 
+# Batched workloads: num_graphs graphs, sizes log-uniform in [n_min, n_max], half Barabasi-Albert
+# (m in {2,4,8,16}), half Watts-Strogatz (k in {6,10,20}, p = 0.1), each with 0-3 planted cliques
+# of 8-64 vertices; all decomposed in one call.
+BATCHES = {
+    "batch4096": dict(num_graphs=4096, n_min=500, n_max=50000, seed=1),
+    "batch256": dict(num_graphs=256, n_min=500, n_max=50000, seed=1),
+}
+
 # Exact pass volume of the reference schedule for each workload (number of count-and-prune
 # passes of the chained single-k runs and the sum of their alive oriented edges).  The engine
 # recomputes both every run and bench.py checks them; the reference arm needs them to scale its
@@ -205,6 +213,87 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+def run_batch(args, world, rank, local):
+    """graphs/s of the batched decomposition (device buffers; e2e through kt_decompose_batch)."""
+    import torch
+
+    import ktruss_gb300 as kt
+
+    dist = world > 1
+    if dist:
+        import torch.distributed as td
+
+        td.init_process_group("nccl")
+    else:
+        td = None
+    torch.cuda.set_device(local)
+    b = BATCHES[args.workload]
+    t0 = time.time()
+    n, u, v, off = kt.gen_batch(b["num_graphs"], b["n_min"], b["n_max"], b["seed"])
+    gen_s = time.time() - t0
+    G = b["num_graphs"]
+    src = np.concatenate([u, v]).astype(np.uint32)
+    dst = np.concatenate([v, u]).astype(np.uint32)
+    N, m = len(src), len(u)
+    eng = kt.Engine(local)
+    eng.reserve(n, N)
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a, np.uint32).view(np.int32)).cuda()
+    d_src, d_dst, d_off = dev(src), dev(dst), dev(off)
+    d_out = torch.empty(N, dtype=torch.int32, device="cuda")
+    d_k = torch.empty(G, dtype=torch.int32, device="cuda")
+    stream = torch.cuda.ExternalStream(eng.stream)
+    torch.cuda.synchronize()
+
+    def step():
+        eng.decompose_batch(d_src.data_ptr(), d_dst.data_ptr(), N, n, d_off.data_ptr(), G, d_out.data_ptr(),
+                            d_k.data_ptr(), sync=False)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    launches0 = eng.stats().kernel_launches
+    if dist:
+        td.barrier()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            step()
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    ms = max_over_ranks(ev0.elapsed_time(ev1) / args.steps, td, "cuda")
+    st = eng.stats()
+    launches = st.kernel_launches - launches0
+    kmax = d_k.cpu().numpy()
+    h_src = torch.from_numpy(src.view(np.int32)).pin_memory().numpy().view(np.uint32)
+    h_dst = torch.from_numpy(dst.view(np.int32)).pin_memory().numpy().view(np.uint32)
+    h_out = torch.empty(N, dtype=torch.int32).pin_memory().numpy().view(np.uint32)
+    kt.decompose_batch(h_src, h_dst, n, off, out=h_out)
+    t1 = time.perf_counter()
+    for _ in range(args.steps):
+        _, k2 = kt.decompose_batch(h_src, h_dst, n, off, out=h_out)
+    e2e_s = max_over_ranks((time.perf_counter() - t1) / args.steps, td, "cuda")
+    if not np.array_equal(k2, kmax.view(np.uint32)):
+        raise RuntimeError("host-buffer and device-buffer batches differ")
+    line = {"metric": "batched k-truss decomposition graphs/s", "value": G * world / (ms * 1e-3),
+            "unit": "graphs/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+            "config": {"workload": f"{args.workload}: {G} graphs, n log-uniform in [{b['n_min']}, {b['n_max']}], "
+                                   "half Barabasi-Albert, half Watts-Strogatz, 0-3 planted cliques each, "
+                                   "one call", "n": n, "m": m, "edges_per_s": m * world / (ms * 1e-3),
+                       "k_max_max": int(kmax.max()), "peel_rounds": st.num_rounds, "peel_levels": st.num_levels,
+                       "phase_ms": {"build": st.build_ms, "support": st.support_ms, "peel": st.peel_ms},
+                       "generation_s": gen_s, "parallelism": f"replicas{world}"},
+            "e2e": {"value": G * world / e2e_s, "unit": "graphs/s", "h2d_bytes_per_step": 8 * N + 4 * (G + 1),
+                    "d2h_bytes_per_step": 4 * N + 4 * G},
+            "gpu_launches": launches, "clocks": clk.summary()}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    eng.close()
+    if dist:
+        td.destroy_process_group()
+
+
 def run_ours(args, world, rank, local):
     import torch
 
@@ -334,13 +423,15 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="rmat20", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="rmat20", choices=sorted(WORKLOADS) + sorted(BATCHES))
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
     world, rank, local = dist_env()
     if args.impl == "reference":
         run_reference(args, world, rank)
+    elif args.workload in BATCHES:
+        run_batch(args, world, rank, local)
     else:
         run_ours(args, world, rank, local)
 

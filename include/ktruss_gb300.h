@@ -195,6 +195,20 @@ int kt_engine_decompose(kt_engine* engine, const uint32_t* d_src, const uint32_t
 int kt_engine_ktruss(kt_engine* engine, const uint32_t* d_src, const uint32_t* d_dst,
                      uint64_t num_entries, uint32_t num_nodes, uint32_t k, uint8_t* d_keep,
                      int sync);
+/* Batched decomposition (no counterpart in the reference): num_graphs graphs in one call, given
+ * as one COO over disjoint vertex ranges — graph g owns vertices [d_vertex_offsets[g],
+ * d_vertex_offsets[g+1]), num_graphs+1 offsets ending at num_nodes, and every entry stays inside
+ * one graph (else KT_ERR_INVALID_ARG).  The batch runs as one graph: one build, one support
+ * count and one persistent peel launch whose work chunks mix all graphs.  Outputs per entry as
+ * in kt_engine_decompose, and d_k_max_per_graph[g] (0 for a graph without edges). */
+int kt_engine_decompose_batch(kt_engine* engine, const uint32_t* d_src, const uint32_t* d_dst,
+                              uint64_t num_entries, uint32_t num_nodes, const uint32_t* d_vertex_offsets,
+                              uint32_t num_graphs, uint32_t* d_truss_per_entry, uint32_t* d_k_max_per_graph,
+                              int sync);
+/* The same with host buffers (copied to and from the device in the call). */
+int kt_decompose_batch(const uint32_t* src, const uint32_t* dst, uint64_t num_entries, uint32_t num_nodes,
+                       const uint32_t* vertex_offsets, uint32_t num_graphs, uint32_t* truss_per_entry,
+                       uint32_t* k_max_per_graph);
 /* Synchronizes the engine stream and fills *stats.  Returns KT_ERR_TIMEOUT if the last peel
  * kernel gave up on a grid barrier. */
 int kt_engine_stats(kt_engine* engine, kt_stats* stats);
@@ -238,6 +252,12 @@ int kt_gen_rgg(uint32_t n, double radius, uint64_t seed, kt_edges* out);
  * (u[i], v[i]) of a graph with num_nodes vertices; the result is canonical again. */
 int kt_plant_cliques(uint32_t num_nodes, const uint32_t* u, const uint32_t* v, uint64_t num_edges,
                      uint32_t count, uint32_t min_size, uint32_t max_size, uint64_t seed, kt_edges* out);
+/* A batch of num_graphs graphs as one edge list over disjoint vertex ranges: graph g owns
+ * vertices [vertex_offsets[g], vertex_offsets[g+1]) (num_graphs+1 offsets written).  Sizes are
+ * log-uniform in [n_min, n_max]; even graphs Barabasi-Albert (m in {2,4,8,16}), odd graphs
+ * Watts-Strogatz (k in {6,10,20}, p = 0.1), each with 0-3 planted cliques of 8-64 vertices. */
+int kt_gen_batch(uint32_t num_graphs, uint32_t n_min, uint32_t n_max, uint64_t seed, kt_edges* out,
+                 uint32_t* vertex_offsets);
 void kt_edges_free(kt_edges* graph);
 
 #ifdef __cplusplus

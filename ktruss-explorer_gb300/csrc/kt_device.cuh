@@ -19,6 +19,7 @@ enum : uint32_t {
     kErrAsymmetric = 1u << 3,  // (u, v) present without (v, u)
     kErrTimeout = 1u << 4,     // a bounded grid-barrier wait expired
     kErrRunaway = 1u << 5,     // the peel loop exceeded its round or level bound
+    kErrCrossGraph = 1u << 6,  // a batch entry joins two different graphs
 };
 
 // Layout of the device control block (uint32 words unless noted).

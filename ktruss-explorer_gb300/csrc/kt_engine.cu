@@ -247,6 +247,7 @@ int kt_engine_destroy(kt_engine* e) {
     cudaSetDevice(e->device);
     if (e->stream) cudaStreamSynchronize(e->stream);
     if (e->arena) cudaFree(e->arena);
+    if (e->aux) cudaFree(e->aux);
     if (e->ctrl) cudaFree(e->ctrl);
     if (e->h_ctrl) cudaFreeHost(e->h_ctrl);
     if (e->ev_start) cudaEventDestroy(e->ev_start);
@@ -354,6 +355,78 @@ int kt_engine_stats(kt_engine* e, kt_stats* stats) {
     e->stats.kernel_launches = e->launches;
     *stats = e->stats;
     return KT_OK;
+}
+
+int kt_engine_decompose_batch(kt_engine* e, const uint32_t* d_src, const uint32_t* d_dst, uint64_t num_entries,
+                              uint32_t num_nodes, const uint32_t* d_vertex_offsets, uint32_t num_graphs,
+                              uint32_t* d_truss_per_entry, uint32_t* d_k_max_per_graph, int sync) {
+    if (!e) return fail(KT_ERR_INVALID_ARG, "kt_engine_decompose_batch: null engine");
+    if (!d_vertex_offsets || !d_k_max_per_graph || num_graphs == 0 ||
+        (num_entries && (!d_src || !d_dst || !d_truss_per_entry)))
+        return fail(KT_ERR_INVALID_ARG, "kt_engine_decompose_batch: null buffer or no graphs");
+    kt::clear_error();
+    int rc = check_cuda(cudaSetDevice(e->device), "cudaSetDevice");
+    if (rc) return rc;
+    // the union of disjoint graphs: its truss numbers are each graph's own
+    if ((rc = run_decompose(e, d_src, d_dst, num_entries, num_nodes, d_truss_per_entry, nullptr))) return rc;
+    if ((rc = kt::emit_graph_kmax(e, d_src, d_dst, d_vertex_offsets, num_graphs, d_truss_per_entry,
+                                  d_k_max_per_graph)))
+        return rc;
+    if (sync) {
+        if ((rc = check_cuda(cudaStreamSynchronize(e->stream), "synchronize"))) return rc;
+        e->stats_ready = false;
+        return kt::finish_stats(e);
+    }
+    return KT_OK;
+}
+
+int kt_decompose_batch(const uint32_t* src, const uint32_t* dst, uint64_t num_entries, uint32_t num_nodes,
+                       const uint32_t* vertex_offsets, uint32_t num_graphs, uint32_t* truss_per_entry,
+                       uint32_t* k_max_per_graph) {
+    if (!vertex_offsets || !k_max_per_graph || num_graphs == 0 || (num_entries && (!src || !dst || !truss_per_entry)))
+        return fail(KT_ERR_INVALID_ARG, "kt_decompose_batch: null buffer or no graphs");
+    for (uint32_t g = 0; g < num_graphs; ++g)
+        if (vertex_offsets[g] > vertex_offsets[g + 1])
+            return fail(KT_ERR_INVALID_ARG, "kt_decompose_batch: vertex offsets decrease at graph %u", g);
+    if (vertex_offsets[num_graphs] != num_nodes)
+        return fail(KT_ERR_INVALID_ARG, "kt_decompose_batch: last vertex offset %u != num_nodes %u",
+                    vertex_offsets[num_graphs], num_nodes);
+    if (num_entries >= 0xffffffffull) return fail(KT_ERR_TOO_LARGE, "more than 2^32-2 entries");
+    kt::clear_error();
+    kt_engine* e = nullptr;
+    int rc;
+    if ((rc = default_engine(&e))) return rc;
+    std::lock_guard<std::mutex> lock(g_default_mu);
+    if ((rc = check_cuda(cudaSetDevice(e->device), "cudaSetDevice"))) return rc;
+    if ((rc = kt::reserve(e, std::max(num_nodes, e->cap_nodes), std::max(num_entries, e->cap_entries)))) return rc;
+    const size_t need = 2 * (size_t)num_graphs + 1;
+    if (e->aux_words < need) {
+        if (e->aux) cudaFree(e->aux);
+        e->aux = nullptr;
+        e->aux_words = 0;
+        if ((rc = check_cuda(cudaMalloc(&e->aux, sizeof(uint32_t) * need), "allocate batch staging"))) return rc;
+        e->aux_words = need;
+    }
+    uint32_t* d_off = e->aux;
+    uint32_t* d_kmax = e->aux + num_graphs + 1;
+    const uint64_t N = num_entries;
+    if ((rc = check_cuda(cudaMemcpyAsync(d_off, vertex_offsets, sizeof(uint32_t) * (num_graphs + 1),
+                                         cudaMemcpyHostToDevice, e->stream), "H2D")))
+        return rc;
+    if (N && ((rc = check_cuda(cudaMemcpyAsync(e->in_src, src, N * 4, cudaMemcpyHostToDevice, e->stream), "H2D")) ||
+              (rc = check_cuda(cudaMemcpyAsync(e->in_dst, dst, N * 4, cudaMemcpyHostToDevice, e->stream), "H2D"))))
+        return rc;
+    if ((rc = run_decompose(e, e->in_src, e->in_dst, N, num_nodes, e->out_u32, nullptr))) return rc;
+    if ((rc = kt::emit_graph_kmax(e, e->in_src, e->in_dst, d_off, num_graphs, e->out_u32, d_kmax))) return rc;
+    if (N && (rc = check_cuda(cudaMemcpyAsync(truss_per_entry, e->out_u32, N * 4, cudaMemcpyDeviceToHost, e->stream),
+                              "D2H")))
+        return rc;
+    if ((rc = check_cuda(cudaMemcpyAsync(k_max_per_graph, d_kmax, sizeof(uint32_t) * num_graphs,
+                                         cudaMemcpyDeviceToHost, e->stream), "D2H")) ||
+        (rc = check_cuda(cudaStreamSynchronize(e->stream), "synchronize")))
+        return rc;
+    e->stats_ready = false;
+    return kt::finish_stats(e);
 }
 
 int kt_decompose(const kt_coo* graph, uint32_t* truss_per_entry, uint32_t* k_max, const kt_config* config) {

@@ -74,6 +74,8 @@ struct kt_engine {
     uint32_t* in_dst = nullptr;
     uint32_t* out_u32 = nullptr;
     uint8_t* out_u8 = nullptr;
+    uint32_t* aux = nullptr;       // batch staging: vertex offsets and per-graph k_max (own allocation)
+    size_t aux_words = 0;
 
     // Current graph.
     uint32_t n = 0;
@@ -115,6 +117,8 @@ int peel_decompose(kt_engine* e);
 int peel_single_k(kt_engine* e, uint32_t k);
 int emit_truss_per_entry(kt_engine* e, uint32_t* d_out, uint32_t* d_k_max);
 int emit_keep(kt_engine* e, uint8_t* d_keep);
+int emit_graph_kmax(kt_engine* e, const uint32_t* d_src, const uint32_t* d_dst, const uint32_t* d_offsets,
+                    uint32_t num_graphs, const uint32_t* d_truss, uint32_t* d_kmax);
 // Reads the peel's control block and round log (stream must be drained); reports timeouts.
 int finish_stats(kt_engine* e);
 // Launches a grid barrier that cannot complete and returns the status it reports.

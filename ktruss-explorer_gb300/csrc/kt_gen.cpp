@@ -18,6 +18,8 @@
 #include "kt_internal.h"
 
 #include <algorithm>
+#include <atomic>
+#include <cmath>
 #include <cstdint>
 #include <cstdlib>
 #include <cstring>
@@ -331,6 +333,89 @@ int kt_plant_cliques(uint32_t num_nodes, const uint32_t* u, const uint32_t* v, u
             for (size_t j = i + 1; j < members.size(); ++j) keys.push_back(pack(members[i], members[j]));
     }
     return finish(keys, num_nodes, out);
+}
+
+int kt_gen_batch(uint32_t num_graphs, uint32_t n_min, uint32_t n_max, uint64_t seed, kt_edges* out,
+                 uint32_t* vertex_offsets) {
+    if (!out || !vertex_offsets || num_graphs == 0 || n_min < 64 || n_max < n_min) return KT_ERR_INVALID_ARG;
+    memset(out, 0, sizeof(*out));
+    // per graph: size log-uniform in [n_min, n_max] (libm exp/log), even graphs Barabasi-Albert with
+    // m in {2,4,8,16}, odd graphs Watts-Strogatz with k in {6,10,20} and p = 0.1; then 0-3 cliques
+    // of 8-64 vertices (capped at the graph size)
+    std::vector<uint32_t> sizes(num_graphs);
+    Rng rng(seed, 7);
+    const double lr = std::log((double)n_max / (double)n_min);
+    uint64_t total_n = 0;
+    for (uint32_t g = 0; g < num_graphs; ++g) {
+        const double u = (double)(rng.at(4ull * g) >> 11) * (1.0 / 9007199254740992.0);
+        uint32_t n = (uint32_t)std::llround((double)n_min * std::exp(u * lr));
+        if (n < n_min) n = n_min;
+        if (n > n_max) n = n_max;
+        sizes[g] = n;
+        vertex_offsets[g] = (uint32_t)total_n;
+        total_n += n;
+        if (total_n > 0xffffffffull) return KT_ERR_TOO_LARGE;
+    }
+    vertex_offsets[num_graphs] = (uint32_t)total_n;
+    std::vector<kt_edges> parts(num_graphs);
+    std::atomic<uint32_t> next{0};
+    std::atomic<int> status{KT_OK};
+    auto work = [&] {
+        for (uint32_t g; (g = next.fetch_add(1)) < num_graphs;) {
+            const uint64_t gs = mix64(seed ^ mix64(0x6a09e667f3bcc909ull + g));
+            const uint32_t n = sizes[g];
+            kt_edges base{};
+            int rc;
+            if ((g & 1) == 0) {
+                static const uint32_t ms[4] = {2, 4, 8, 16};
+                rc = kt_gen_ba(n, ms[rng.at(4ull * g + 1) & 3], gs, &base);
+            } else {
+                static const uint32_t ks[3] = {6, 10, 20};
+                rc = kt_gen_ws(n, ks[bounded(rng.at(4ull * g + 1), 3)], 0.1, gs, &base);
+            }
+            if (rc == KT_OK) {
+                const uint32_t cliques = bounded(rng.at(4ull * g + 2), 4);
+                const uint32_t hi = std::min<uint32_t>(64, n);
+                if (cliques) {
+                    kt_edges with{};
+                    rc = kt_plant_cliques(n, base.u, base.v, base.num_edges, cliques, std::min<uint32_t>(8, hi), hi,
+                                          gs ^ 0x3c6ef372fe94f82bull, &with);
+                    kt_edges_free(&base);
+                    base = with;
+                }
+            }
+            if (rc != KT_OK) status.store(rc);
+            parts[g] = base;
+        }
+    };
+    std::vector<std::thread> th;
+    for (unsigned t = 0; t < worker_count(); ++t) th.emplace_back(work);
+    for (auto& x : th) x.join();
+    if (status.load() != KT_OK) {
+        for (auto& p : parts) kt_edges_free(&p);
+        return status.load();
+    }
+    uint64_t m = 0;
+    for (auto& p : parts) m += p.num_edges;
+    out->num_nodes = (uint32_t)total_n;
+    out->num_edges = m;
+    out->u = (uint32_t*)malloc(sizeof(uint32_t) * (m ? m : 1));
+    out->v = (uint32_t*)malloc(sizeof(uint32_t) * (m ? m : 1));
+    if (!out->u || !out->v) {
+        kt_edges_free(out);
+        for (auto& p : parts) kt_edges_free(&p);
+        return KT_ERR_HOST_ALLOC;
+    }
+    uint64_t w = 0;
+    for (uint32_t g = 0; g < num_graphs; ++g) {
+        const uint32_t off = vertex_offsets[g];
+        for (uint64_t i = 0; i < parts[g].num_edges; ++i, ++w) {
+            out->u[w] = parts[g].u[i] + off;
+            out->v[w] = parts[g].v[i] + off;
+        }
+        kt_edges_free(&parts[g]);
+    }
+    return KT_OK;
 }
 
 void kt_edges_free(kt_edges* g) {

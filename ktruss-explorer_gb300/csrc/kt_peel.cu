@@ -546,6 +546,43 @@ __global__ void k_emit_keep(const uint32_t* __restrict__ entry_eid, uint64_t ent
 
 __global__ void k_copy_u32(uint32_t* dst, const uint32_t* src) { *dst = *src; }
 
+// Per-graph k_max of a batch: entry i belongs to the graph whose vertex range holds its source;
+// lanes of a warp with the same graph combine before the atomic.  An entry whose endpoints lie in
+// different graphs sets kErrCrossGraph.
+__global__ void k_graph_kmax(const uint32_t* __restrict__ src, const uint32_t* __restrict__ dst, uint64_t entries,
+                             const uint32_t* __restrict__ offsets, uint32_t num_graphs,
+                             const uint32_t* __restrict__ truss, uint32_t* __restrict__ kmax,
+                             uint32_t* __restrict__ ctrl) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t g = 0xffffffffu, t = 0, err = 0;
+    if (i < entries) {
+        const uint32_t s = src[i], d = dst[i];
+        // graph of s: last g with offsets[g] <= s
+        uint32_t lo = 0, len = num_graphs + 1;
+        while (len > 0) {
+            const uint32_t half = len >> 1;
+            if (offsets[lo + half] <= s) {
+                lo += half + 1;
+                len -= half + 1;
+            } else {
+                len = half;
+            }
+        }
+        g = lo - 1;
+        if (g >= num_graphs || d < offsets[g] || d >= offsets[g + 1]) {
+            err = kErrCrossGraph;
+            g = 0xffffffffu;
+        } else {
+            t = truss[i];
+        }
+    }
+    const uint32_t peers = __match_any_sync(kFullMask, g);
+    const uint32_t best = __reduce_max_sync(peers, t);
+    if (g != 0xffffffffu && lane_id() == (uint32_t)(__ffs(peers) - 1)) atomicMax(&kmax[g], best);
+    err = __reduce_or_sync(kFullMask, err);
+    if (err && lane_id() == 0) atomicOr(&ctrl[kCtrlError], err);
+}
+
 __global__ void k_fill_edges(uint32_t m, uint32_t value, uint32_t* __restrict__ rnd) {
     uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j < m) rnd[j] = value;
@@ -664,6 +701,16 @@ int emit_truss_per_entry(kt_engine* e, uint32_t* d_out, uint32_t* d_k_max) {
     return KT_OK;
 }
 
+int emit_graph_kmax(kt_engine* e, const uint32_t* d_src, const uint32_t* d_dst, const uint32_t* d_offsets,
+                    uint32_t num_graphs, const uint32_t* d_truss, uint32_t* d_kmax) {
+    int rc = check_cuda(cudaMemsetAsync(d_kmax, 0, sizeof(uint32_t) * num_graphs, e->stream), "clear k_max");
+    if (rc || !e->entries) return rc;
+    k_graph_kmax<<<grid_for(e->entries), kThreads, 0, e->stream>>>(d_src, d_dst, e->entries, d_offsets, num_graphs,
+                                                                   d_truss, d_kmax, e->ctrl);
+    count_launch(e);
+    return check_launch(e, "k_graph_kmax");
+}
+
 int emit_keep(kt_engine* e, uint8_t* d_keep) {
     if (!e->entries) return KT_OK;
     k_emit_keep<<<grid_for(e->entries), kThreads, 0, e->stream>>>(e->entry_eid, e->entries, e->rnd, d_keep);
@@ -695,6 +742,7 @@ int finish_stats(kt_engine* e) {
     const uint32_t err = e->h_ctrl[kCtrlError];
     if (err & kErrTimeout) return fail(KT_ERR_TIMEOUT, "a grid barrier wait of the peel kernel expired");
     if (err & kErrRunaway) return fail(KT_ERR_INTERNAL, "the peel kernel exceeded its round or level bound");
+    if (err & kErrCrossGraph) return fail(KT_ERR_INVALID_ARG, "a batch entry joins vertices of two different graphs");
     const uint64_t m = e->m;
     e->stats.triangles = ((uint64_t)e->h_ctrl[kCtrlTriHi] << 32 | e->h_ctrl[kCtrlTriLo]) / 3;
     e->stats.k_max = m ? (e->peel_mode == 0 ? e->h_ctrl[kPKmax] : 0) : 0;

@@ -115,6 +115,12 @@ def lib() -> ctypes.CDLL:
                                        ctypes.c_int]
         L.kt_engine_stats.argtypes = [_VP, ctypes.POINTER(Stats)]
         L.kt_engine_selftest_barrier_timeout.argtypes = [_VP, ctypes.c_uint64]
+        L.kt_engine_decompose_batch.argtypes = [_VP, _VP, _VP, ctypes.c_uint64, ctypes.c_uint32, _VP, ctypes.c_uint32,
+                                                _VP, _VP, ctypes.c_int]
+        L.kt_decompose_batch.argtypes = [_U32P, _U32P, ctypes.c_uint64, ctypes.c_uint32, _U32P, ctypes.c_uint32,
+                                         _U32P, _U32P]
+        L.kt_gen_batch.argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint64,
+                                   ctypes.POINTER(_Edges), _U32P]
         L.kt_decompose_noalloc.argtypes = [_VP, _VP, ctypes.c_uint64, ctypes.c_uint32, _VP, _VP, _VP]
         L.kt_engine_level_log.argtypes = [_VP, _U32P, _U32P, _U32P, _U32P, ctypes.c_uint32, _U32P]
         L.kt_engine_round_log.argtypes = [_VP, _U32P, _U32P, _U32P, ctypes.c_uint32, _U32P]
@@ -323,6 +329,11 @@ class Engine:
         _check(lib().kt_engine_decompose(self._h, d_src, d_dst, num_entries, num_nodes, d_truss, d_k_max or None,
                                          int(sync)))
 
+    def decompose_batch(self, d_src: int, d_dst: int, num_entries: int, num_nodes: int, d_offsets: int,
+                        num_graphs: int, d_truss: int, d_k_max: int, sync: bool = True) -> None:
+        _check(lib().kt_engine_decompose_batch(self._h, d_src, d_dst, num_entries, num_nodes, d_offsets, num_graphs,
+                                               d_truss, d_k_max, int(sync)))
+
     def ktruss(self, d_src: int, d_dst: int, num_entries: int, num_nodes: int, k: int, d_keep: int,
                sync: bool = True) -> None:
         _check(lib().kt_engine_ktruss(self._h, d_src, d_dst, num_entries, num_nodes, k & 0xFFFFFFFF, d_keep,
@@ -353,6 +364,36 @@ class Engine:
         s = Stats()
         _check(lib().kt_engine_stats(self._h, ctypes.byref(s)))
         return s
+
+
+def decompose_batch(src, dst, num_nodes: int, vertex_offsets, out: Optional[np.ndarray] = None):
+    """Batched decomposition of graphs on disjoint vertex ranges (host buffers).
+    Returns (truss per entry, k_max per graph)."""
+    src = np.ascontiguousarray(src, np.uint32)
+    dst = np.ascontiguousarray(dst, np.uint32)
+    off = np.ascontiguousarray(vertex_offsets, np.uint32)
+    G = len(off) - 1
+    if out is None:
+        out = np.zeros(max(len(src), 1), np.uint32)
+    kmax = np.zeros(G, np.uint32)
+    _check(lib().kt_decompose_batch(src.ctypes.data_as(_U32P), dst.ctypes.data_as(_U32P), len(src), num_nodes,
+                                    off.ctypes.data_as(_U32P), G, out.ctypes.data_as(_U32P),
+                                    kmax.ctypes.data_as(_U32P)))
+    return out[: len(src)], kmax
+
+
+def gen_batch(num_graphs: int, n_min: int, n_max: int, seed: int = 1):
+    """(num_nodes, u, v, vertex_offsets) of a seeded batch of BA / WS graphs with planted cliques."""
+    e = _Edges()
+    off = np.zeros(num_graphs + 1, np.uint32)
+    _check(lib().kt_gen_batch(num_graphs, n_min, n_max, seed, ctypes.byref(e), off.ctypes.data_as(_U32P)))
+    try:
+        k = e.num_edges
+        u = np.ctypeslib.as_array(e.u, shape=(k,)).copy() if k else np.zeros(0, np.uint32)
+        v = np.ctypeslib.as_array(e.v, shape=(k,)).copy() if k else np.zeros(0, np.uint32)
+        return e.num_nodes, u, v, off
+    finally:
+        lib().kt_edges_free(ctypes.byref(e))
 
 
 def decompose_noalloc(d_src: int, d_dst: int, num_entries: int, num_nodes: int, d_truss: int, d_k_max: int = 0,

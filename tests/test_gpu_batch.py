@@ -1,0 +1,65 @@
+"""Batched decomposition: many graphs on disjoint vertex ranges in one call; every graph's truss
+numbers and k_max must equal its own decomposition (checked against the oracle per graph)."""
+import numpy as np
+import pytest
+
+import ktruss_gb300 as kt
+import oracle
+from conftest import both_directions
+
+pytestmark = pytest.mark.gpu
+
+
+def _per_graph_oracle(n, u, v, off):
+    truss = np.zeros(len(u), np.uint32)
+    kmax = np.zeros(len(off) - 1, np.uint32)
+    gid = np.searchsorted(off, u, side="right") - 1
+    for g in range(len(off) - 1):
+        sel = np.nonzero(gid == g)[0]
+        if len(sel) == 0:
+            continue
+        lu, lv = u[sel] - off[g], v[sel] - off[g]
+        s, d = both_directions(lu, lv)
+        r = oracle.decompose(int(off[g + 1] - off[g]), s, d, method="peel")
+        truss[sel] = r["truss"][: len(sel)]
+        kmax[g] = r["k_max"]
+    return truss, kmax
+
+
+@pytest.mark.parametrize("seed", [5, 6])
+def test_batch_matches_each_graph(seed):
+    n, u, v, off = kt.gen_batch(48, 64, 2500, seed)
+    src, dst = both_directions(u, v)
+    truss, kmax = kt.decompose_batch(src, dst, n, off)
+    ref_t, ref_k = _per_graph_oracle(n, u, v, off)
+    assert np.array_equal(truss[: len(u)], ref_t) and np.array_equal(truss[len(u):], ref_t)
+    assert np.array_equal(kmax, ref_k)
+
+
+def test_batch_with_empty_graphs_and_device_api():
+    torch = pytest.importorskip("torch")
+    # three graphs: K5, no edges, a triangle
+    u = np.array([0, 0, 0, 0, 1, 1, 1, 2, 2, 3, 7, 7, 8], np.uint32)
+    v = np.array([1, 2, 3, 4, 2, 3, 4, 3, 4, 4, 8, 9, 9], np.uint32)
+    off = np.array([0, 5, 7, 10], np.uint32)
+    src, dst = both_directions(u, v)
+    eng = kt.Engine(0)
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a, np.uint32).view(np.int32)).cuda()
+    d_src, d_dst, d_off = t(src), t(dst), t(off)
+    d_out = torch.zeros(len(src), dtype=torch.int32, device="cuda")
+    d_k = torch.full((3,), 99, dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    eng.decompose_batch(d_src.data_ptr(), d_dst.data_ptr(), len(src), 10, d_off.data_ptr(), 3, d_out.data_ptr(),
+                        d_k.data_ptr())
+    assert d_k.cpu().tolist() == [5, 0, 3]
+    assert set(d_out.cpu().tolist()) == {5, 3}
+    eng.close()
+
+
+def test_batch_rejects_cross_graph_entries():
+    u = np.array([0, 1], np.uint32)
+    v = np.array([1, 3], np.uint32)
+    src, dst = both_directions(u, v)
+    with pytest.raises(kt.KtrussError) as ei:
+        kt.decompose_batch(src, dst, 4, np.array([0, 2, 4], np.uint32))
+    assert ei.value.status == 1
