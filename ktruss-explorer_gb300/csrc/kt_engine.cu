@@ -78,10 +78,11 @@ size_t carve(kt_engine* e, char* base, uint32_t n, uint64_t N, bool staging) {
     e->round_size = c.take<uint32_t>(e->cap_rounds);
     e->round_level = c.take<uint32_t>(e->cap_rounds);
     e->round_ns = c.take<uint32_t>(e->cap_rounds);
-    e->level_k = c.take<uint32_t>(e->cap_rounds);
-    e->level_alive = c.take<uint32_t>(e->cap_rounds);
-    e->level_ns = c.take<uint32_t>(e->cap_rounds);
-    e->level_front = c.take<uint32_t>(e->cap_rounds);
+    e->cap_levels = (uint32_t)std::min<uint64_t>(m + 2, 1u << 16);
+    e->level_k = c.take<uint32_t>(e->cap_levels);
+    e->level_alive = c.take<uint32_t>(e->cap_levels);
+    e->level_ns = c.take<uint32_t>(e->cap_levels);
+    e->level_front = c.take<uint32_t>(e->cap_levels);
     e->hist = c.take<uint32_t>(hist_words);
     e->hist_words = hist_words;
     e->scan_tmp = c.take<uint32_t>(scan_words);
@@ -336,7 +337,7 @@ int kt_engine_level_log(kt_engine* e, uint32_t* k, uint32_t* alive, uint32_t* ns
     if ((rc = kt::finish_stats(e))) return rc;
     const uint32_t L = e->stats.num_levels;
     *num_levels = L;
-    const uint32_t c = std::min<uint32_t>(std::min<uint32_t>(cap, L), e->cap_rounds);
+    const uint32_t c = std::min<uint32_t>(std::min<uint32_t>(cap, L), e->cap_levels);
     if (c == 0) return KT_OK;
     uint32_t* dst[4] = {k, alive, ns, frontier};
     uint32_t* src[4] = {e->level_k, e->level_alive, e->level_ns, e->level_front};

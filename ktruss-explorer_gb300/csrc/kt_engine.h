@@ -64,6 +64,7 @@ struct kt_engine {
     uint32_t* round_size = nullptr;
     uint32_t* round_level = nullptr;
     uint32_t* round_ns = nullptr;
+    uint32_t cap_levels = 0;
     uint32_t* level_k = nullptr;      // per-level log (k, alive, start time, first frontier)
     uint32_t* level_alive = nullptr;
     uint32_t* level_ns = nullptr;

@@ -83,6 +83,7 @@ struct PeelParams {
     uint32_t* level_ns;
     uint32_t* level_front;
     uint32_t cap_rounds;
+    uint32_t cap_levels;
     uint32_t n, m, big_row;
     uint32_t single_k;  // 0: full decomposition; >= 3: the k of a single-k truss
     uint64_t timeout_ns;
@@ -432,7 +433,7 @@ __global__ void __launch_bounds__(kPeelThreads, 1) k_peel(PeelParams P) {
         }
         const uint32_t km2 = k - 2;
         uint32_t E = ld_acquire(ctrl + kPEdges + (rr & 3)), B = ld_acquire(ctrl + kPBigCount + (rr & 3));
-        if (leader && level < P.cap_rounds) {
+        if (leader && level < P.cap_levels) {
             P.level_k[level] = k;
             P.level_alive[level] = P.single_k ? P.m : ld_acquire(ctrl + kPLAlive + ls);
             P.level_ns[level] = (uint32_t)(global_ns() - level_t0);
@@ -623,6 +624,7 @@ int launch_peel(kt_engine* e, uint32_t single_k) {
     P.level_ns = e->level_ns;
     P.level_front = e->level_front;
     P.cap_rounds = e->cap_rounds;
+    P.cap_levels = e->cap_levels;
     P.n = e->n;
     P.m = e->m;
     P.big_row = e->big_row;
