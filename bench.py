@@ -54,6 +54,9 @@ BATCHES = {
     "batch4096": dict(num_graphs=4096, n_min=500, n_max=50000, seed=1),
     "batch256": dict(num_graphs=256, n_min=500, n_max=50000, seed=1),
 }
+# The autotuner times its candidate schedules on a separate sample of the same distribution
+# (other seed), never on the graphs that are measured.
+TUNE_SAMPLE = dict(num_graphs=256, seed=1001)
 
 # Exact pass volume of the reference schedule for each workload (number of count-and-prune
 # passes of the chained single-k runs and the sum of their alive oriented edges).  The engine
@@ -213,6 +216,39 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+def parse_schedule(text):
+    """'default', 'auto' or 'G,W,C' (support group, chunk width, compaction percent)."""
+    if text in ("default", "auto"):
+        return text
+    g, w, c = (int(x) for x in text.split(","))
+    return (g, w, c)
+
+
+def choose_schedule(args, eng, kt, sample):
+    """Sets the engine's schedule (and the host-buffer engine's) from --schedule; 'auto' runs the
+    autotuner on `sample()` = (n, src, dst) device tensors.  Returns the config record."""
+    import torch
+
+    choice = parse_schedule(args.schedule)
+    rec = {"mode": args.schedule if isinstance(choice, str) else "fixed"}
+    if choice == "auto":
+        n, d_src, d_dst = sample()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        best, table = eng.autotune(d_src.data_ptr(), d_dst.data_ptr(), d_src.numel(), n)
+        rec["tuning_s"] = time.perf_counter() - t0
+        rec["candidates"] = len(table)
+        rec["default_ms"] = next(ms for s, ms in table if s.as_tuple() == kt.schedule_default().as_tuple())
+        rec["best_ms"] = min(ms for _, ms in table)
+        choice = best.as_tuple()
+    elif choice == "default":
+        choice = kt.schedule_default().as_tuple()
+    eng.set_schedule(*choice)
+    kt.set_schedule(*choice)
+    rec["support_group"], rec["chunk_width"], rec["compact_percent"] = choice
+    return rec
+
+
 def run_batch(args, world, rank, local):
     """graphs/s of the batched decomposition (device buffers; e2e through kt_decompose_batch)."""
     import torch
@@ -242,6 +278,12 @@ def run_batch(args, world, rank, local):
     d_out = torch.empty(N, dtype=torch.int32, device="cuda")
     d_k = torch.empty(G, dtype=torch.int32, device="cuda")
     stream = torch.cuda.ExternalStream(eng.stream)
+
+    def tune_sample():
+        ns, us, vs, _ = kt.gen_batch(TUNE_SAMPLE["num_graphs"], b["n_min"], b["n_max"], TUNE_SAMPLE["seed"])
+        return ns, dev(np.concatenate([us, vs])), dev(np.concatenate([vs, us]))
+
+    sched = choose_schedule(args, eng, kt, tune_sample)
     torch.cuda.synchronize()
 
     def step():
@@ -283,7 +325,8 @@ def run_batch(args, world, rank, local):
                                    "one call", "n": n, "m": m, "edges_per_s": m * world / (ms * 1e-3),
                        "k_max_max": int(kmax.max()), "peel_rounds": st.num_rounds, "peel_levels": st.num_levels,
                        "phase_ms": {"build": st.build_ms, "support": st.support_ms, "peel": st.peel_ms},
-                       "generation_s": gen_s, "parallelism": f"replicas{world}"},
+                       "generation_s": gen_s, "parallelism": f"replicas{world}", "schedule": sched,
+                       "l2": "input entries 2x4x2m bytes > L2 (129 MB)"},
             "e2e": {"value": G * world / e2e_s, "unit": "graphs/s", "h2d_bytes_per_step": 8 * N + 4 * (G + 1),
                     "d2h_bytes_per_step": 4 * N + 4 * G},
             "gpu_launches": launches, "clocks": clk.summary()}
@@ -314,6 +357,14 @@ def run_ours(args, world, rank, local):
     d_out = torch.empty(N, dtype=torch.int32, device="cuda")
     d_k = torch.zeros(1, dtype=torch.int32, device="cuda")
     stream = torch.cuda.ExternalStream(eng.stream)
+
+    def tune_sample():
+        w = WORKLOADS[args.workload]
+        ns, us, vs = kt.gen_rmat(w["scale"] - 2, w["ef"], w["a"], w["b"], w["c"], w["seed"] + 1000)
+        dev = lambda a: torch.from_numpy(np.ascontiguousarray(a, np.uint32).view(np.int32)).cuda()
+        return ns, dev(np.concatenate([us, vs])), dev(np.concatenate([vs, us]))
+
+    sched = choose_schedule(args, eng, kt, tune_sample)
     torch.cuda.synchronize()  # the engine stream does not order after torch's copies
 
     def step():
@@ -390,7 +441,8 @@ def run_ours(args, world, rank, local):
                        "parallelism": f"replicas{world}", "l2": "input entries 2x4x2m bytes > L2 (129 MB)",
                        "phase_ms": {"build": statistics.mean(build_ms), "support": sup_ms,
                                     "peel": statistics.mean(peel_ms)},
-                       "peel_phase_ms": st.as_dict()["peel_phase_ms"], "compactions": st.compactions},
+                       "peel_phase_ms": st.as_dict()["peel_phase_ms"], "compactions": st.compactions,
+                       "schedule": sched},
             "e2e": {"value": replica_throughput(m, world, e2e_s * 1e3), "unit": "edges/s", "h2d_bytes_per_step": 8 * N,
                     "d2h_bytes_per_step": 4 * N},
             "gpu_launches": launches // args.steps * args.steps,
@@ -426,7 +478,13 @@ def main():
     ap.add_argument("--workload", default="rmat20", choices=sorted(WORKLOADS) + sorted(BATCHES))
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--schedule", default=None,
+                    help="kernel schedule: default, auto (autotune on a separate sample of the same "
+                         "distribution) or G,W,C; default: auto for batches, default for single graphs")
     args = ap.parse_args()
+    if args.schedule is None:
+        args.schedule = "auto" if args.workload in BATCHES else "default"
+    parse_schedule(args.schedule)
     world, rank, local = dist_env()
     if args.impl == "reference":
         run_reference(args, world, rank)

@@ -176,6 +176,19 @@ typedef struct kt_stats {
     float peel_kernel_ms;        /* CUDA-event time of the peel kernel launch alone            */
 } kt_stats;
 
+/* Schedule of the engine's kernels (no counterpart in the reference, whose tuning knobs are the
+ * -b/-t block and tile sizes).  Every schedule gives the same result; only the time differs. */
+typedef struct kt_schedule {
+    uint32_t support_group;    /* lanes per oriented edge in the support count: 4, 8, 16 or 32   */
+    uint32_t chunk_width;      /* row entries per peel work chunk (lanes per chunk): 8, 16 or 32  */
+    uint32_t compact_percent;  /* compact the adjacency rows at a level start once the alive
+                                  edges are below this percentage of the count at the last
+                                  compaction: 1..99, or 0 = never                                */
+} kt_schedule;
+
+/* The default schedule {8, 32, 85}. */
+kt_schedule kt_schedule_default(void);
+
 /* Creates an engine on `device` with its own non-blocking CUDA stream. */
 int kt_engine_create(int device, kt_engine** out);
 int kt_engine_destroy(kt_engine* engine);
@@ -222,6 +235,28 @@ int kt_engine_round_log(kt_engine* engine, uint32_t* size, uint32_t* level, uint
  * and the size of its first frontier (any pointer may be NULL). */
 int kt_engine_level_log(kt_engine* engine, uint32_t* k, uint32_t* alive, uint32_t* ns, uint32_t* frontier,
                         uint32_t cap, uint32_t* num_levels);
+/* Sets the schedule of the engine's later calls (KT_ERR_INVALID_ARG for a value outside the
+ * ranges above); kt_engine_get_schedule reads it. */
+int kt_engine_set_schedule(kt_engine* engine, const kt_schedule* schedule);
+int kt_engine_get_schedule(kt_engine* engine, kt_schedule* schedule);
+/* Schedule of the engine behind the host-buffer entry points (kt_ktruss, kt_decompose,
+ * kt_decompose_batch). */
+int kt_set_schedule(const kt_schedule* schedule);
+int kt_get_schedule(kt_schedule* schedule);
+/* The autotuner's built-in grid of schedules: support_group {4, 8, 16, 32} x chunk_width
+ * {8, 16, 32} x compact_percent {0, 70, 85} (36).  Writes min(36, cap) schedules to `out` (may be
+ * NULL) and returns 36. */
+uint32_t kt_schedule_grid(kt_schedule* out, uint32_t cap);
+/* Autotuner (no counterpart in the reference).  Decomposes the given device graph — or a batch
+ * given as the union of its graphs — once per candidate schedule and `repeats` times each
+ * (>= 1), and keeps the candidate with the least device time of support count plus peel (CUDA
+ * events; the CSR build does not depend on the schedule).  candidates: num_candidates schedules,
+ * or NULL for the built-in grid.  ms (optional): the least time of each candidate.  On return the
+ * engine runs with the fastest schedule, also written to *best (optional).  Callers tune on a
+ * sample of the graphs they will run and reuse the schedule for the rest. */
+int kt_engine_autotune(kt_engine* engine, const uint32_t* d_src, const uint32_t* d_dst, uint64_t num_entries,
+                       uint32_t num_nodes, const kt_schedule* candidates, uint32_t num_candidates,
+                       uint32_t repeats, float* ms, kt_schedule* best);
 /* Self-test of the bounded device waits: launches a grid barrier that one block never reaches,
  * with a wait limit of timeout_ns (at most 5 s).  Returns KT_ERR_TIMEOUT when the wait expired
  * and the kernel returned as designed; the engine stays usable afterwards. */

@@ -50,7 +50,7 @@ enum : uint32_t {
     kPBigCount = 28,   // [4] long-row slots of the round
     kPLAlive = 32,     // [4] alive edges after the level scan
     kPLMin = 36,       // [4] minimum support over them
-    kPLFront = 40,     // [4] frontier of the level's first round
+    kPLMinId = 40,     // [4] smallest alive edge id at the level scan (later scans start there)
     kPCompactions = 44,
     kPPhaseNs = 48,    // [6] u64 nanoseconds per phase kind (init, level scan, collect,
                        //     compaction, mark, process), measured by block 0 barrier to barrier

@@ -300,6 +300,105 @@ int kt_engine_ktruss(kt_engine* e, const uint32_t* d_src, const uint32_t* d_dst,
     return KT_OK;
 }
 
+kt_schedule kt_schedule_default(void) { return kt_schedule{8, 32, 85}; }
+
+int kt_engine_set_schedule(kt_engine* e, const kt_schedule* s) {
+    kt::clear_error();
+    if (!e || !s) return fail(KT_ERR_INVALID_ARG, "kt_engine_set_schedule: null argument");
+    const uint32_t g = s->support_group, w = s->chunk_width;
+    if (g != 4 && g != 8 && g != 16 && g != 32)
+        return fail(KT_ERR_INVALID_ARG, "support_group must be 4, 8, 16 or 32 (got %u)", g);
+    if (w != 8 && w != 16 && w != 32) return fail(KT_ERR_INVALID_ARG, "chunk_width must be 8, 16 or 32 (got %u)", w);
+    if (s->compact_percent > 99)
+        return fail(KT_ERR_INVALID_ARG, "compact_percent must be 0..99 (got %u)", s->compact_percent);
+    e->sched = *s;
+    return KT_OK;
+}
+
+int kt_engine_get_schedule(kt_engine* e, kt_schedule* s) {
+    kt::clear_error();
+    if (!e || !s) return fail(KT_ERR_INVALID_ARG, "kt_engine_get_schedule: null argument");
+    *s = e->sched;
+    return KT_OK;
+}
+
+int kt_set_schedule(const kt_schedule* s) {
+    kt_engine* e = nullptr;
+    int rc = default_engine(&e);
+    if (rc) return rc;
+    std::lock_guard<std::mutex> lock(g_default_mu);
+    return kt_engine_set_schedule(e, s);
+}
+
+int kt_get_schedule(kt_schedule* s) {
+    kt_engine* e = nullptr;
+    int rc = default_engine(&e);
+    if (rc) return rc;
+    std::lock_guard<std::mutex> lock(g_default_mu);
+    return kt_engine_get_schedule(e, s);
+}
+
+uint32_t kt_schedule_grid(kt_schedule* out, uint32_t cap) {
+    static const uint32_t groups[] = {4, 8, 16, 32}, widths[] = {8, 16, 32}, compact[] = {0, 70, 85};
+    uint32_t i = 0;
+    for (uint32_t g : groups)
+        for (uint32_t w : widths)
+            for (uint32_t c : compact) {
+                if (out && i < cap) out[i] = kt_schedule{g, w, c};
+                ++i;
+            }
+    return i;
+}
+
+int kt_engine_autotune(kt_engine* e, const uint32_t* d_src, const uint32_t* d_dst, uint64_t num_entries,
+                       uint32_t num_nodes, const kt_schedule* candidates, uint32_t num_candidates, uint32_t repeats,
+                       float* ms, kt_schedule* best) {
+    kt::clear_error();
+    if (!e) return fail(KT_ERR_INVALID_ARG, "kt_engine_autotune: null engine");
+    if (num_entries && (!d_src || !d_dst)) return fail(KT_ERR_INVALID_ARG, "kt_engine_autotune: null buffer");
+    if (repeats == 0) return fail(KT_ERR_INVALID_ARG, "kt_engine_autotune: repeats must be >= 1");
+    kt_schedule grid[36];
+    if (!candidates) {
+        num_candidates = kt_schedule_grid(grid, 36);
+        candidates = grid;
+    }
+    if (num_candidates == 0) return fail(KT_ERR_INVALID_ARG, "kt_engine_autotune: no candidates");
+    const kt_schedule saved = e->sched;
+    int rc = check_cuda(cudaSetDevice(e->device), "cudaSetDevice");
+    if (rc) return rc;
+    uint32_t best_i = 0;
+    float best_ms = 0;
+    for (uint32_t i = 0; i < num_candidates; ++i) {
+        if ((rc = kt_engine_set_schedule(e, &candidates[i]))) break;
+        float t_min = 0;
+        for (uint32_t r = 0; r < repeats && !rc; ++r) {
+            // the rows are compacted in place while peeling, so every run builds the CSR again
+            if ((rc = kt::build_graph(e, d_src, d_dst, num_entries, num_nodes)) || (rc = record(e, e->ev_built)) ||
+                (rc = kt::count_support(e)) || (rc = kt::peel_decompose(e)) || (rc = record(e, e->ev_stop)) ||
+                (rc = check_cuda(cudaEventSynchronize(e->ev_stop), "synchronize")))
+                break;
+            float t = 0;
+            if ((rc = check_cuda(cudaEventElapsedTime(&t, e->ev_built, e->ev_stop), "elapsed time")) ||
+                (rc = kt::finish_stats(e)))
+                break;
+            t_min = r == 0 || t < t_min ? t : t_min;
+        }
+        if (rc) break;
+        if (ms) ms[i] = t_min;
+        if (i == 0 || t_min < best_ms) {
+            best_ms = t_min;
+            best_i = i;
+        }
+    }
+    if (rc) {
+        e->sched = saved;
+        return rc;
+    }
+    e->sched = candidates[best_i];
+    if (best) *best = candidates[best_i];
+    return KT_OK;
+}
+
 int kt_engine_selftest_barrier_timeout(kt_engine* e, uint64_t timeout_ns) {
     if (!e) return fail(KT_ERR_INVALID_ARG, "kt_engine_selftest_barrier_timeout: null engine");
     if (timeout_ns == 0 || timeout_ns > 5000000000ull)

@@ -50,9 +50,6 @@ constexpr int kThreads = 256;          // helper kernels
 #endif
 constexpr int kPeelThreads = KT_PEEL_THREADS;  // persistent kernel: one block per SM
 constexpr int kBatch = KT_PEEL_BATCH;  // row entries in flight per thread
-// Rows are compacted once the alive edges fall below this fraction (num/den) of the count at
-// the last compaction.
-constexpr uint64_t kCompactNum = 17, kCompactDen = 20;
 constexpr uint64_t kPeelTimeoutNs = 10ull * 1000 * 1000 * 1000;
 
 inline uint32_t grid_for(uint64_t n, int threads = kThreads) {
@@ -85,6 +82,9 @@ struct PeelParams {
     uint32_t cap_rounds;
     uint32_t cap_levels;
     uint32_t n, m, big_row;
+    uint32_t cw_shift;  // log2 of the chunk width (row entries per work chunk): 3, 4 or 5
+    uint32_t compact_num;  // rows are compacted once alive edges < compact_num/100 of the count
+                           // at the last compaction (0: never)
     uint32_t single_k;  // 0: full decomposition; >= 3: the k of a single-k truss
     uint64_t timeout_ns;
 };
@@ -95,8 +95,8 @@ constexpr uint32_t kFirstChunk = 0x80000000u;
 constexpr uint32_t kNullChunk = 0xffffffffu;
 
 // Queues edge e for round rr if `take`: stamps it, and splits the walk of its shorter row into
-// chunks of up to 32 entries, one warp each, described by {edge, other endpoint y, row position,
-// entry count | kFirstChunk on the edge's first chunk}.  Rows are only compacted at level
+// chunks of up to W = 1 << cw_shift entries (8, 16 or 32), each walked by W lanes, described by
+// {edge, other endpoint y, row position, entry count | kFirstChunk on the edge's first chunk}.  Rows are only compacted at level
 // starts, so the row measured here is the row walked.  Called by all 32 lanes of a warp
 // together: chunk slots are claimed with one atomic per warp.  If the chunk buffer is full, the
 // claimed slots are nulled and the edges go to the block-walked queue instead.
@@ -112,7 +112,7 @@ __device__ __forceinline__ void push_edges(const PeelParams& P, uint32_t e, bool
         y = ux ? v : u;
         base = P.s_ptr[ux ? u : v];
         len = ux ? lu : lv;
-        nch = len ? (len + 31) >> 5 : 1;
+        nch = len ? (len + (1u << P.cw_shift) - 1) >> P.cw_shift : 1;
     }
     const uint32_t lane = lane_id(), slot = rr & 3;
     uint32_t incl = nch;
@@ -133,8 +133,8 @@ __device__ __forceinline__ void push_edges(const PeelParams& P, uint32_t e, bool
         if (take) {
             const uint32_t c0 = cb + incl - nch;
             for (uint32_t c = 0; c < nch; ++c) {
-                const uint32_t off = c << 5;
-                const uint32_t cnt = len > off ? min(32u, len - off) : 0u;
+                const uint32_t off = c << P.cw_shift;
+                const uint32_t cnt = len > off ? min(1u << P.cw_shift, len - off) : 0u;
                 ch[c0 + c] = make_uint4(e, y, base + off, cnt | (c == 0 ? kFirstChunk : 0u));
             }
         }
@@ -149,7 +149,8 @@ __device__ __forceinline__ void push_edges(const PeelParams& P, uint32_t e, bool
 }
 
 // Entries of a removed edge e's shorter row (vertex x): called by all 32 lanes of a warp
-// together; lane l handles positions base + t0 + l + j*step (j < NB) that are below base + len,
+// together (each lane may serve a different edge); the lane at position `pos` of its group
+// handles row positions base + t0 + pos + j*step (j < NB) that are below base + len,
 // so that the memory chains of different entries overlap.  For a neighbour w of x, edge (x,w) is
 // s_eid at the entry and edge (y,w) is found by a binary search in an oriented row (w in N+(y)
 // if w > y, else y in N+(w)); the NB searches advance in lockstep.  Edge states during round r:
@@ -159,13 +160,12 @@ __device__ __forceinline__ void push_edges(const PeelParams& P, uint32_t e, bool
 // an edge whose support falls from k-2 to k-3 is queued for round r+1.
 template <int NB>
 __device__ __forceinline__ void peel_entries(const PeelParams& P, uint32_t e, uint32_t y, uint32_t base, uint32_t len,
-                                             uint32_t t0, uint32_t step, uint32_t r, uint32_t km2) {
-    const uint32_t lane = lane_id();
+                                             uint32_t t0, uint32_t pos, uint32_t step, uint32_t r, uint32_t km2) {
     uint32_t a[NB], lo[NB], n[NB], end[NB], tgt[NB];
     bool act[NB];
 #pragma unroll
     for (int j = 0; j < NB; ++j) {
-        const uint32_t t = t0 + lane + (uint32_t)j * step;
+        const uint32_t t = t0 + pos + (uint32_t)j * step;
         act[j] = t < len;
         uint32_t w = y;
         if (act[j]) {
@@ -307,9 +307,9 @@ __device__ void compact_rows(const PeelParams& P, uint32_t r_done, uint32_t* war
 
 // Collects a level's first frontier: alive edges with support <= thr, queued for round rr
 // (removed edges hold kDead and never qualify).
-__device__ __forceinline__ void collect(const PeelParams& P, uint32_t thr, uint32_t rr, uint64_t tid,
+__device__ __forceinline__ void collect(const PeelParams& P, uint32_t thr, uint32_t rr, uint32_t start, uint64_t tid,
                                         uint64_t nthreads) {
-    for (uint64_t j0 = tid - lane_id(); j0 < P.m; j0 += nthreads) {
+    for (uint64_t j0 = start + tid - lane_id(); j0 < P.m; j0 += nthreads) {
         const uint64_t j = j0 + lane_id();
         push_edges(P, (uint32_t)j, j < P.m && P.sup[j] <= thr, rr);
     }
@@ -365,7 +365,7 @@ __global__ void __launch_bounds__(kPeelThreads, 1) k_peel(PeelParams P) {
         }
         if (leader) ctrl[kPNext + ((rr + 1) & 3)] = ctrl[kPBigCount + ((rr + 1) & 3)] = ctrl[kPEdges + ((rr + 1) & 3)] = 0;
         // compact the rows once the alive edges have dropped enough since the last compaction
-        if (live * kCompactDen < live_at_compaction * kCompactNum) {
+        if (live * 100 < live_at_compaction * P.compact_num) {
             compact_rows(P, r, warp_cnt);
             if (!grid_barrier(ctrl, nblocks, P.timeout_ns)) return;
             KT_PHASE(3)
@@ -380,14 +380,17 @@ __global__ void __launch_bounds__(kPeelThreads, 1) k_peel(PeelParams P) {
                 const uint32_t z = (level + 2) & 3;
                 ctrl[kPLAlive + z] = 0;
                 ctrl[kPLMin + z] = 0xffffffffu;
+                ctrl[kPLMinId + z] = 0xffffffffu;
             }
-            // stream the whole support array (16-byte loads, four edges per lane; removed edges
-            // hold kDead)
-            uint32_t n_alive = 0, mn = kDead;
+            // stream the support array (16-byte loads, four edges per lane; removed edges hold
+            // kDead) from the smallest edge id alive at the previous level's scan: edges below it
+            // are all removed, and low ids (rows of low-degree vertices) go first
+            const uint32_t start = level ? ld_acquire(ctrl + kPLMinId + ((level + 3) & 3)) & ~3u : 0u;
+            uint32_t n_alive = 0, mn = kDead, min_id = kDead;
             const uint4* sup4 = reinterpret_cast<const uint4*>(P.sup);
             const uint64_t m4 = ((uint64_t)P.m + 3) / 4;
             constexpr int kScanUnroll = 2;  // 16-byte loads in flight per lane
-            for (uint64_t i0 = tid - lane; i0 < m4; i0 += nthreads * kScanUnroll) {
+            for (uint64_t i0 = (start >> 2) + tid - lane; i0 < m4; i0 += nthreads * kScanUnroll) {
                 uint4 q4[kScanUnroll];
 #pragma unroll
                 for (int u = 0; u < kScanUnroll; ++u) {
@@ -405,6 +408,7 @@ __global__ void __launch_bounds__(kPeelThreads, 1) k_peel(PeelParams P) {
                         if (sj != kDead) {
                             ++n_alive;
                             mn = sj < mn ? sj : mn;
+                            min_id = (uint32_t)j < min_id ? (uint32_t)j : min_id;
                         }
                         push_edges(P, (uint32_t)j, sj != kDead && sj <= kg - 3, rr);
                     }
@@ -412,22 +416,24 @@ __global__ void __launch_bounds__(kPeelThreads, 1) k_peel(PeelParams P) {
             }
             n_alive = __reduce_add_sync(kFullMask, n_alive);
             mn = __reduce_min_sync(kFullMask, mn);
+            min_id = __reduce_min_sync(kFullMask, min_id);
             if (lane == 0) {
                 if (n_alive) atomicAdd(ctrl + kPLAlive + ls, n_alive);
                 if (mn != kDead) atomicMin(ctrl + kPLMin + ls, mn);
+                if (min_id != kDead) atomicMin(ctrl + kPLMinId + ls, min_id);
             }
             if (!grid_barrier(ctrl, nblocks, P.timeout_ns)) return;
             KT_PHASE(1)
             if (ld_acquire(ctrl + kPLAlive + ls) == 0) break;
             k = ld_acquire(ctrl + kPLMin + ls) + 3;
             if (k != kg) {
-                collect(P, k - 3, rr, tid, nthreads);
+                collect(P, k - 3, rr, ld_acquire(ctrl + kPLMinId + ls), tid, nthreads);
                 if (!grid_barrier(ctrl, nblocks, P.timeout_ns)) return;
                 KT_PHASE(2)
             }
         } else {
             k = P.single_k;
-            collect(P, k - 3, rr, tid, nthreads);
+            collect(P, k - 3, rr, 0u, tid, nthreads);
             if (!grid_barrier(ctrl, nblocks, P.timeout_ns)) return;
             KT_PHASE(2)
         }
@@ -457,22 +463,38 @@ __global__ void __launch_bounds__(kPeelThreads, 1) k_peel(PeelParams P) {
                     P.round_level[rounds] = k;
                 }
             }
-            // chunks: one warp per chunk of up to 32 row entries
+            // chunks: a warp takes 32 / W chunks at a time, W lanes per chunk of up to W row
+            // entries
             {
                 const uint4* ch = P.ch[r & 1];
-                for (uint32_t c = gwarp; c < C; c += nwarps) {
-                    const uint4 d = ch[c];
-                    if (d.x == kNullChunk) continue;
-                    if ((d.w & kFirstChunk) && lane == 0) {
+                const uint32_t per_warp = 32u >> P.cw_shift, pos = lane & ((1u << P.cw_shift) - 1);
+                const uint32_t mine = lane >> P.cw_shift;
+                for (uint32_t c0 = gwarp * per_warp; c0 < C; c0 += nwarps * per_warp) {
+                    const uint32_t c = c0 + mine;
+                    const uint4 d = c < C ? ch[c] : make_uint4(kNullChunk, 0, 0, 0);
+                    const bool real = d.x != kNullChunk;
+                    if (real && (d.w & kFirstChunk) && pos == 0) {
                         P.tr[d.x] = k - 1;
                         P.sup[d.x] = kDead;
                     }
-                    peel_entries<1>(P, d.x, d.y, d.z, d.w & ~kFirstChunk, 0, 32, r, km2);
+                    peel_entries<1>(P, real ? d.x : 0u, d.y, d.z, real ? d.w & ~kFirstChunk : 0u, 0, pos, 32, r, km2);
                 }
             }
-            // edges that did not fit the chunk buffer: one block per edge, or several blocks per
-            // edge when they are few
-            if (B) {
+            // edges that did not fit the chunk buffer: one warp per edge when there are at least
+            // as many edges as warps; else one block per edge, or several blocks per edge
+            if (B >= nwarps) {
+                const uint32_t* bq = P.big[r & 1];
+                for (uint32_t i = gwarp; i < B; i += nwarps) {
+                    const uint32_t e = bq[i];
+                    uint32_t y, base, len;
+                    slot_context(P, e, &y, &base, &len);
+                    if (lane == 0) {
+                        P.tr[e] = k - 1;
+                        P.sup[e] = kDead;
+                    }
+                    for (uint32_t t0 = 0; t0 < len; t0 += 32) peel_entries<1>(P, e, y, base, len, t0, lane, 32, r, km2);
+                }
+            } else if (B) {
                 const uint32_t* bq = P.big[r & 1];
                 const uint32_t parts = B >= nblocks ? 1u : nblocks / B;
                 const uint32_t units = B >= nblocks ? B : B * parts;
@@ -487,7 +509,7 @@ __global__ void __launch_bounds__(kPeelThreads, 1) k_peel(PeelParams P) {
                     }
                     const uint32_t wofs = threadIdx.x & ~31u;
                     for (uint32_t t0 = part * blockDim.x + wofs; t0 < len; t0 += parts * blockDim.x)
-                        peel_entries<1>(P, e, y, base, len, t0, parts * blockDim.x, r, km2);
+                        peel_entries<1>(P, e, y, base, len, t0, lane, parts * blockDim.x, r, km2);
                 }
             }
             if (!grid_barrier(ctrl, nblocks, P.timeout_ns)) return;
@@ -523,7 +545,8 @@ __global__ void k_barrier_probe(uint32_t* ctrl, uint64_t timeout_ns) {
 
 __global__ void k_init_peel_ctrl(uint32_t* ctrl) {
     const uint32_t i = threadIdx.x;
-    if (i >= kPBarCount && i < kCtrlWords) ctrl[i] = (i >= kPLMin && i < kPLMin + 4) ? 0xffffffffu : 0u;
+    if (i >= kPBarCount && i < kCtrlWords)
+        ctrl[i] = (i >= kPLMin && i < kPLMin + 4) || (i >= kPLMinId && i < kPLMinId + 4) ? 0xffffffffu : 0u;
 }
 
 __global__ void k_sum_support(const uint32_t* __restrict__ sup, uint32_t m, unsigned long long* __restrict__ total) {
@@ -628,6 +651,8 @@ int launch_peel(kt_engine* e, uint32_t single_k) {
     P.n = e->n;
     P.m = e->m;
     P.big_row = e->big_row;
+    P.cw_shift = e->sched.chunk_width == 8 ? 3u : e->sched.chunk_width == 16 ? 4u : 5u;
+    P.compact_num = e->sched.compact_percent;
     P.single_k = single_k;
     P.timeout_ns = kPeelTimeoutNs;
     void* args[] = {&P};

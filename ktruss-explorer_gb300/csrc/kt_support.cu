@@ -2,7 +2,8 @@
 //
 // Replaces count_triangles_kernel of the reference (kernel_ddc.cu:11-54): there one thread
 // merges the two out-lists of its edge and issues three atomics per triangle.  Here each
-// oriented edge (u,v), u < v in rank order, is handled by a group of G lanes.  Only the part
+// oriented edge (u,v), u < v in rank order, is handled by a group of G lanes (G = 4, 8, 16 or
+// 32, the schedule's support_group).  Only the part
 // of N+(u) above v can hold a common neighbour, and it starts right after the edge itself in
 // u's row, so the intersection is  S = o_col[j+1 .. o_ptr[u+1])  with  L = N+(v).  Lanes stride
 // over the shorter list and binary-search the longer one; for a triangle (u,v,w) found at
@@ -67,12 +68,16 @@ int count_support(kt_engine* e) {
     if (e->m == 0) return KT_OK;
     int rc = check_cuda(cudaMemsetAsync(e->sup, 0, sizeof(uint32_t) * e->m, e->stream), "clear support");
     if (rc) return rc;
-    constexpr int G = 8;
-    uint64_t groups_needed = e->m;
-    uint64_t blocks = (groups_needed * G + kThreads - 1) / kThreads;
-    uint64_t max_blocks = (uint64_t)e->num_sms * 16;
+    const uint32_t G = e->sched.support_group;
+    uint64_t blocks = ((uint64_t)e->m * G + kThreads - 1) / kThreads;
+    const uint64_t max_blocks = (uint64_t)e->num_sms * 16;
     if (blocks > max_blocks) blocks = max_blocks;
-    k_support<G><<<(uint32_t)blocks, kThreads, 0, e->stream>>>(e->o_ptr, e->o_col, e->e_src, e->m, e->sup);
+    switch (G) {
+        case 4: k_support<4><<<(uint32_t)blocks, kThreads, 0, e->stream>>>(e->o_ptr, e->o_col, e->e_src, e->m, e->sup); break;
+        case 16: k_support<16><<<(uint32_t)blocks, kThreads, 0, e->stream>>>(e->o_ptr, e->o_col, e->e_src, e->m, e->sup); break;
+        case 32: k_support<32><<<(uint32_t)blocks, kThreads, 0, e->stream>>>(e->o_ptr, e->o_col, e->e_src, e->m, e->sup); break;
+        default: k_support<8><<<(uint32_t)blocks, kThreads, 0, e->stream>>>(e->o_ptr, e->o_col, e->e_src, e->m, e->sup); break;
+    }
     count_launch(e);
     return check_launch(e, "k_support");
 }

@@ -78,6 +78,19 @@ class Stats(ctypes.Structure):
         return d
 
 
+class Schedule(ctypes.Structure):
+    """kt_schedule: lanes per edge of the support count, row entries per peel chunk, and the
+    alive-edge percentage below which rows are compacted (0 = never).  Results never depend on it."""
+    _fields_ = [("support_group", ctypes.c_uint32), ("chunk_width", ctypes.c_uint32),
+                ("compact_percent", ctypes.c_uint32)]
+
+    def as_tuple(self) -> tuple:
+        return (self.support_group, self.chunk_width, self.compact_percent)
+
+    def __repr__(self) -> str:
+        return "Schedule(support_group=%d, chunk_width=%d, compact_percent=%d)" % self.as_tuple()
+
+
 _LIB = None
 _U32P = ctypes.POINTER(ctypes.c_uint32)
 _VP = ctypes.c_void_p
@@ -124,6 +137,17 @@ def lib() -> ctypes.CDLL:
         L.kt_decompose_noalloc.argtypes = [_VP, _VP, ctypes.c_uint64, ctypes.c_uint32, _VP, _VP, _VP]
         L.kt_engine_level_log.argtypes = [_VP, _U32P, _U32P, _U32P, _U32P, ctypes.c_uint32, _U32P]
         L.kt_engine_round_log.argtypes = [_VP, _U32P, _U32P, _U32P, ctypes.c_uint32, _U32P]
+        L.kt_schedule_default.restype = Schedule
+        L.kt_schedule_default.argtypes = []
+        L.kt_engine_set_schedule.argtypes = [_VP, ctypes.POINTER(Schedule)]
+        L.kt_engine_get_schedule.argtypes = [_VP, ctypes.POINTER(Schedule)]
+        L.kt_set_schedule.argtypes = [ctypes.POINTER(Schedule)]
+        L.kt_get_schedule.argtypes = [ctypes.POINTER(Schedule)]
+        L.kt_schedule_grid.argtypes = [ctypes.POINTER(Schedule), ctypes.c_uint32]
+        L.kt_schedule_grid.restype = ctypes.c_uint32
+        L.kt_engine_autotune.argtypes = [_VP, _VP, _VP, ctypes.c_uint64, ctypes.c_uint32, ctypes.POINTER(Schedule),
+                                         ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(ctypes.c_float),
+                                         ctypes.POINTER(Schedule)]
         for g in ("kt_gen_rmat",):
             getattr(L, g).argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_double, ctypes.c_double,
                                       ctypes.c_double, ctypes.c_uint64, ctypes.POINTER(_Edges)]
@@ -339,6 +363,28 @@ class Engine:
         _check(lib().kt_engine_ktruss(self._h, d_src, d_dst, num_entries, num_nodes, k & 0xFFFFFFFF, d_keep,
                                       int(sync)))
 
+    def set_schedule(self, support_group: int = 8, chunk_width: int = 32, compact_percent: int = 85) -> None:
+        s = Schedule(support_group, chunk_width, compact_percent)
+        _check(lib().kt_engine_set_schedule(self._h, ctypes.byref(s)))
+
+    def schedule(self) -> Schedule:
+        s = Schedule()
+        _check(lib().kt_engine_get_schedule(self._h, ctypes.byref(s)))
+        return s
+
+    def autotune(self, d_src: int, d_dst: int, num_entries: int, num_nodes: int, candidates=None,
+                 repeats: int = 1) -> tuple:
+        """Times every candidate schedule (default: the built-in grid) on this device graph and
+        keeps the fastest; returns (best Schedule, [(Schedule, ms), ...])."""
+        cands = list(candidates) if candidates is not None else schedule_grid()
+        arr = (Schedule * len(cands))(*[Schedule(*c.as_tuple()) if isinstance(c, Schedule) else Schedule(*c)
+                                        for c in cands])
+        ms = (ctypes.c_float * len(cands))()
+        best = Schedule()
+        _check(lib().kt_engine_autotune(self._h, d_src, d_dst, num_entries, num_nodes, arr, len(cands), repeats, ms,
+                                        ctypes.byref(best)))
+        return best, [(arr[i], ms[i]) for i in range(len(cands))]
+
     def selftest_barrier_timeout(self, timeout_ns: int) -> int:
         """Status of a grid barrier that cannot complete (KT_ERR_TIMEOUT = 11 when correct)."""
         return lib().kt_engine_selftest_barrier_timeout(self._h, timeout_ns)
@@ -364,6 +410,30 @@ class Engine:
         s = Stats()
         _check(lib().kt_engine_stats(self._h, ctypes.byref(s)))
         return s
+
+
+def schedule_default() -> Schedule:
+    return lib().kt_schedule_default()
+
+
+def set_schedule(support_group: int = 8, chunk_width: int = 32, compact_percent: int = 85) -> None:
+    """Schedule of the engine behind the host-buffer calls (ktruss, decompose, decompose_batch)."""
+    s = Schedule(support_group, chunk_width, compact_percent)
+    _check(lib().kt_set_schedule(ctypes.byref(s)))
+
+
+def get_schedule() -> Schedule:
+    s = Schedule()
+    _check(lib().kt_get_schedule(ctypes.byref(s)))
+    return s
+
+
+def schedule_grid() -> list:
+    """The autotuner's built-in candidate schedules."""
+    n = lib().kt_schedule_grid(None, 0)
+    arr = (Schedule * n)()
+    lib().kt_schedule_grid(arr, n)
+    return [arr[i] for i in range(n)]
 
 
 def decompose_batch(src, dst, num_nodes: int, vertex_offsets, out: Optional[np.ndarray] = None):

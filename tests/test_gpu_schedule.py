@@ -1,0 +1,127 @@
+"""Every kernel schedule (support group, chunk width, compaction threshold) gives the oracle's
+truss numbers bit for bit; invalid schedules are rejected."""
+import itertools
+
+import numpy as np
+import pytest
+
+import ktruss_gb300 as kt
+import oracle
+from conftest import both_directions
+
+pytestmark = pytest.mark.gpu
+
+GRAPHS = [
+    ("rmat13", lambda: kt.gen_rmat(13, 16, 0.57, 0.19, 0.19, 11)),
+    ("ba6000_cliques", lambda: kt.plant_cliques(*kt.gen_ba(6000, 4, 12), 3, 16, 48, 13)),
+    ("ws8000", lambda: kt.gen_ws(8000, 10, 0.1, 14)),
+]
+
+SCHEDULES = list(itertools.product((4, 8, 16, 32), (8, 16, 32), (0, 50, 85)))
+
+
+@pytest.fixture(scope="module")
+def torch():
+    return pytest.importorskip("torch")
+
+
+@pytest.mark.parametrize("name,make", GRAPHS, ids=[g[0] for g in GRAPHS])
+def test_every_schedule_matches_oracle(name, make, torch):
+    n, u, v = make()
+    src, dst = both_directions(u, v)
+    ref = oracle.decompose(n, src, dst, method="peel")
+    eng = kt.Engine(0)
+    d_src = torch.from_numpy(src.view(np.int32)).cuda()
+    d_dst = torch.from_numpy(dst.view(np.int32)).cuda()
+    d_out = torch.empty(len(src), dtype=torch.int32, device="cuda")
+    d_k = torch.zeros(1, dtype=torch.int32, device="cuda")
+    for g, w, c in SCHEDULES:
+        eng.set_schedule(g, w, c)
+        assert eng.schedule().as_tuple() == (g, w, c)
+        d_out.fill_(-1)
+        torch.cuda.synchronize()  # the engine runs on its own stream
+        eng.decompose(d_src.data_ptr(), d_dst.data_ptr(), len(src), n, d_out.data_ptr(), d_k.data_ptr())
+        assert int(d_k.item()) == ref["k_max"], (g, w, c)
+        assert np.array_equal(d_out.cpu().numpy().view(np.uint32), ref["truss"]), (g, w, c)
+        st = eng.stats()
+        assert st.compactions == 0 or c != 0
+
+
+@pytest.mark.parametrize("w", [8, 16])
+def test_single_k_with_narrow_chunks(w, torch):
+    n, u, v = kt.plant_cliques(*kt.gen_ba(5000, 8, 21), 2, 20, 40, 22)
+    src, dst = both_directions(u, v)
+    ref = oracle.decompose(n, src, dst, method="peel")
+    eng = kt.Engine(0)
+    eng.set_schedule(16, w, 85)
+    d_src = torch.from_numpy(src.view(np.int32)).cuda()
+    d_dst = torch.from_numpy(dst.view(np.int32)).cuda()
+    keep = torch.empty(len(src), dtype=torch.uint8, device="cuda")
+    torch.cuda.synchronize()
+    for k in (3, 5, ref["k_max"], ref["k_max"] + 1):
+        eng.ktruss(d_src.data_ptr(), d_dst.data_ptr(), len(src), n, k, keep.data_ptr())
+        assert np.array_equal(keep.cpu().numpy().astype(bool), ref["truss"] >= k), k
+
+
+def test_batch_with_narrow_chunks(torch):
+    n, u, v, off = kt.gen_batch(24, 500, 4000, 31)
+    src, dst = both_directions(u, v)
+    eng = kt.Engine(0)
+    eng.set_schedule(4, 8, 50)
+    d_src = torch.from_numpy(src.view(np.int32)).cuda()
+    d_dst = torch.from_numpy(dst.view(np.int32)).cuda()
+    d_off = torch.from_numpy(off.view(np.int32)).cuda()
+    d_out = torch.empty(len(src), dtype=torch.int32, device="cuda")
+    d_k = torch.zeros(len(off) - 1, dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    eng.decompose_batch(d_src.data_ptr(), d_dst.data_ptr(), len(src), n, d_off.data_ptr(), len(off) - 1,
+                        d_out.data_ptr(), d_k.data_ptr())
+    ref = oracle.decompose(n, src, dst, method="peel")
+    assert np.array_equal(d_out.cpu().numpy().view(np.uint32), ref["truss"])
+
+
+@pytest.mark.parametrize("bad", [(2, 32, 85), (64, 32, 85), (8, 4, 85), (8, 64, 85), (8, 32, 100)])
+def test_invalid_schedule_rejected(bad):
+    eng = kt.Engine(0)
+    before = eng.schedule().as_tuple()
+    with pytest.raises(kt.KtrussError) as ei:
+        eng.set_schedule(*bad)
+    assert ei.value.status == 1  # KT_ERR_INVALID_ARG
+    assert eng.schedule().as_tuple() == before
+
+
+def _clique_union(sizes):
+    us, vs, base = [], [], 0
+    for s in sizes:
+        iu, iv = np.triu_indices(s, 1)
+        us.append(iu + base)
+        vs.append(iv + base)
+        base += s
+    return base, np.concatenate(us).astype(np.uint32), np.concatenate(vs).astype(np.uint32)
+
+
+@pytest.mark.parametrize("sizes", [[20] * 300, [100, 100, 64]], ids=["many_small", "few_large"])
+@pytest.mark.parametrize("w", [8, 32])
+def test_chunk_buffer_overflow(sizes, w, torch):
+    """A level whose whole frontier is every edge of many cliques needs more chunks than the
+    buffer holds (m + 4096 on an engine sized for this graph): the rest is walked by warps (many
+    edges) or blocks (few edges).  Every edge of a c-clique has truss number c."""
+    n, u, v = _clique_union(sizes)
+    m = len(u)
+    chunks = sum((s * (s - 1) // 2) * -(-(s - 1) // w) for s in sizes)
+    if w == 8:
+        assert chunks > m + 4096  # the buffer overflows
+    src, dst = both_directions(u, v)
+    expect = np.concatenate([np.full(s * (s - 1) // 2, s, np.uint32) for s in sizes])
+    eng = kt.Engine(0)
+    eng.reserve(n, len(src))
+    eng.set_schedule(8, w, 85)
+    d_src = torch.from_numpy(src.view(np.int32)).cuda()
+    d_dst = torch.from_numpy(dst.view(np.int32)).cuda()
+    d_out = torch.empty(len(src), dtype=torch.int32, device="cuda")
+    d_k = torch.zeros(1, dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    eng.decompose(d_src.data_ptr(), d_dst.data_ptr(), len(src), n, d_out.data_ptr(), d_k.data_ptr())
+    out = d_out.cpu().numpy().view(np.uint32)
+    assert int(d_k.item()) == max(sizes)
+    assert np.array_equal(out[:m], expect) and np.array_equal(out[m:], expect)

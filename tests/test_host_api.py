@@ -162,3 +162,13 @@ def test_cli_missing_graph_fails(tmp_path):
         pytest.skip("CLI not built")
     r = subprocess.run([kt.CLI_PATH, "-g", str(tmp_path / "nope.tsv"), "-v", "0"], capture_output=True, text=True)
     assert r.returncode == 1 and "cannot open" in r.stderr
+
+
+def test_default_schedule():
+    assert kt.schedule_default().as_tuple() == (8, 32, 85)
+
+
+def test_schedule_grid():
+    grid = [s.as_tuple() for s in kt.schedule_grid()]
+    assert len(grid) == 36 and len(set(grid)) == 36
+    assert kt.schedule_default().as_tuple() in grid
