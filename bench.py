@@ -45,6 +45,9 @@ WORKLOADS = {
     "rmat20": dict(scale=20, ef=16, a=0.57, b=0.19, c=0.19, seed=1),
     "rmat18": dict(scale=18, ef=16, a=0.57, b=0.19, c=0.19, seed=1),
     "rmat16": dict(scale=16, ef=16, a=0.57, b=0.19, c=0.19, seed=1),
+    # stress: R-MAT scale 24, edge factor 32, same (a,b,c,d), plus 16 planted cliques of 64-512
+    # random vertices (deep peeling, k_max >= 64)
+    "rmat24": dict(scale=24, ef=32, a=0.57, b=0.19, c=0.19, seed=1, cliques=(16, 64, 512)),
 }
 
 # Batched workloads: num_graphs graphs, sizes log-uniform in [n_min, n_max], half Barabasi-Albert
@@ -81,6 +84,9 @@ def make_graph(name):
 
     w = WORKLOADS[name]
     n, u, v = kt.gen_rmat(w["scale"], w["ef"], w["a"], w["b"], w["c"], w["seed"])
+    if "cliques" in w:
+        count, lo, hi = w["cliques"]
+        n, u, v = kt.plant_cliques(n, u, v, count, lo, hi, w["seed"] + 7)
     src = np.concatenate([u, v]).astype(np.uint32)
     dst = np.concatenate([v, u]).astype(np.uint32)
     return n, len(u), src, dst
@@ -217,11 +223,12 @@ def run_reference(args, world, rank):
 
 
 def parse_schedule(text):
-    """'default', 'auto' or 'G,W,C' (support group, chunk width, compaction percent)."""
+    """'default', 'auto' or 'G,W,C,R' (support group, chunk width, compaction percent, recount
+    percent)."""
     if text in ("default", "auto"):
         return text
-    g, w, c = (int(x) for x in text.split(","))
-    return (g, w, c)
+    g, w, c, r = (int(x) for x in text.split(","))
+    return (g, w, c, r)
 
 
 def choose_schedule(args, eng, kt, sample):
@@ -245,7 +252,7 @@ def choose_schedule(args, eng, kt, sample):
         choice = kt.schedule_default().as_tuple()
     eng.set_schedule(*choice)
     kt.set_schedule(*choice)
-    rec["support_group"], rec["chunk_width"], rec["compact_percent"] = choice
+    rec["support_group"], rec["chunk_width"], rec["compact_percent"], rec["recount_percent"] = choice
     return rec
 
 
@@ -456,12 +463,20 @@ def run_ours(args, world, rank, local):
             "clocks": clk.summary()}
     if rank == 0 and world == 1 and not args.no_cpu:
         s, rate = cpu_sample(n, src, dst, args.cpu_budget, None)
+    else:
+        rate = None
+    if rate == 0:
+        line["cpu_baseline"] = {"value": None, "unit": "edges/s", "cores": 1, "kind": "port",
+                                "sample": f"no triangle count of the reference's first pass finished its first "
+                                          f"4096 edges within {args.cpu_budget:.0f} s (graph set-up included)"}
+    elif rate:
         t_full = st.plain_alive_sum / rate
         line["cpu_baseline"] = {"value": m / t_full, "unit": "edges/s", "cores": 1, "kind": "port",
-                                "sample": (f"first {s['passes']} of {st.plain_passes} count-and-prune passes of "
-                                           f"the reference's chained decomposition ({s['alive_sum']} of "
-                                           f"{st.plain_alive_sum} alive-edge visits) in {s['seconds']:.1f} s, "
-                                           f"scaled by alive-edge volume")}
+                                "sample": (f"first {s['passes']} complete of {st.plain_passes} count-and-prune "
+                                           f"passes of the reference's chained decomposition ({s['alive_sum']} of "
+                                           f"{st.plain_alive_sum} alive-edge visits, a cut pass's merged edges "
+                                           f"included) in {s['seconds']:.1f} s with graph set-up, scaled by "
+                                           f"alive-edge volume")}
     if rank == 0:
         print(json.dumps(line), flush=True)
     eng.close()
@@ -480,7 +495,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--schedule", default=None,
                     help="kernel schedule: default, auto (autotune on a separate sample of the same "
-                         "distribution) or G,W,C; default: auto for batches, default for single graphs")
+                         "distribution) or G,W,C,R; default: auto for batches, default for single graphs")
     args = ap.parse_args()
     if args.schedule is None:
         args.schedule = "auto" if args.workload in BATCHES else "default"

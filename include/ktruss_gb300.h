@@ -184,9 +184,14 @@ typedef struct kt_schedule {
     uint32_t compact_percent;  /* compact the adjacency rows at a level start once the alive
                                   edges are below this percentage of the count at the last
                                   compaction: 1..99, or 0 = never                                */
+    uint32_t recount_percent;  /* a peel round whose frontier holds at least this percentage of
+                                  the alive edges removes it at once and recounts the support of
+                                  the surviving edges from scratch (the reference's full
+                                  recount) instead of decrementing it per destroyed triangle
+                                  (its affected-edge recount, made exact): 1..100, or 0 = never */
 } kt_schedule;
 
-/* The default schedule {8, 32, 85}. */
+/* The default schedule {8, 32, 85, 0}. */
 kt_schedule kt_schedule_default(void);
 
 /* Creates an engine on `device` with its own non-blocking CUDA stream. */
@@ -243,9 +248,9 @@ int kt_engine_get_schedule(kt_engine* engine, kt_schedule* schedule);
  * kt_decompose_batch). */
 int kt_set_schedule(const kt_schedule* schedule);
 int kt_get_schedule(kt_schedule* schedule);
-/* The autotuner's built-in grid of schedules: support_group {4, 8, 16, 32} x chunk_width
- * {8, 16, 32} x compact_percent {0, 70, 85} (36).  Writes min(36, cap) schedules to `out` (may be
- * NULL) and returns 36. */
+/* The autotuner's built-in grid of schedules: support_group {4, 8, 16} x chunk_width
+ * {8, 16, 32} x compact_percent {0, 85} x recount_percent {0, 50} (36).  Writes min(36, cap)
+ * schedules to `out` (may be NULL) and returns 36. */
 uint32_t kt_schedule_grid(kt_schedule* out, uint32_t cap);
 /* Autotuner (no counterpart in the reference).  Decomposes the given device graph — or a batch
  * given as the union of its graphs — once per candidate schedule and `repeats` times each

@@ -46,7 +46,6 @@ enum : uint32_t {
     kPKmax = 18,
     kPRounds = 19,
     kPLevels = 20,
-    kPNext = 24,       // [4] pushes into the next frontier
     kPBigCount = 28,   // [4] long-row slots of the round
     kPLAlive = 32,     // [4] alive edges after the level scan
     kPLMin = 36,       // [4] minimum support over them
@@ -55,7 +54,9 @@ enum : uint32_t {
     kPPhaseNs = 48,    // [6] u64 nanoseconds per phase kind (init, level scan, collect,
                        //     compaction, mark, process), measured by block 0 barrier to barrier
     kPEdges = 60,      // [4] edges queued for the round (chunked or long-row)
-    kCtrlWords = 64,
+    kPChunks = 64,     // [4] u64 (words 64..71): work chunks claimed for the round; 64 bits
+                       //     because a frontier of most edges can need more than 2^32 chunks
+    kCtrlWords = 80,
 };
 
 __device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }
@@ -86,6 +87,12 @@ inline uint32_t ceil_div(uint64_t a, uint64_t b) { return (uint32_t)((a + b - 1)
 __device__ __forceinline__ uint32_t ld_acquire(const uint32_t* p) {
     uint32_t v;
     asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long* p) {
+    unsigned long long v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
     return v;
 }
 

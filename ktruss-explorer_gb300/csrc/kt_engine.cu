@@ -300,7 +300,7 @@ int kt_engine_ktruss(kt_engine* e, const uint32_t* d_src, const uint32_t* d_dst,
     return KT_OK;
 }
 
-kt_schedule kt_schedule_default(void) { return kt_schedule{8, 32, 85}; }
+kt_schedule kt_schedule_default(void) { return kt_schedule{8, 32, 85, 0}; }
 
 int kt_engine_set_schedule(kt_engine* e, const kt_schedule* s) {
     kt::clear_error();
@@ -311,6 +311,8 @@ int kt_engine_set_schedule(kt_engine* e, const kt_schedule* s) {
     if (w != 8 && w != 16 && w != 32) return fail(KT_ERR_INVALID_ARG, "chunk_width must be 8, 16 or 32 (got %u)", w);
     if (s->compact_percent > 99)
         return fail(KT_ERR_INVALID_ARG, "compact_percent must be 0..99 (got %u)", s->compact_percent);
+    if (s->recount_percent > 100)
+        return fail(KT_ERR_INVALID_ARG, "recount_percent must be 0..100 (got %u)", s->recount_percent);
     e->sched = *s;
     return KT_OK;
 }
@@ -339,14 +341,15 @@ int kt_get_schedule(kt_schedule* s) {
 }
 
 uint32_t kt_schedule_grid(kt_schedule* out, uint32_t cap) {
-    static const uint32_t groups[] = {4, 8, 16, 32}, widths[] = {8, 16, 32}, compact[] = {0, 70, 85};
+    static const uint32_t groups[] = {4, 8, 16}, widths[] = {8, 16, 32}, compact[] = {0, 85}, recount[] = {0, 50};
     uint32_t i = 0;
     for (uint32_t g : groups)
         for (uint32_t w : widths)
-            for (uint32_t c : compact) {
-                if (out && i < cap) out[i] = kt_schedule{g, w, c};
-                ++i;
-            }
+            for (uint32_t c : compact)
+                for (uint32_t rc : recount) {
+                    if (out && i < cap) out[i] = kt_schedule{g, w, c, rc};
+                    ++i;
+                }
     return i;
 }
 

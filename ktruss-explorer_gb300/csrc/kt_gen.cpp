@@ -316,11 +316,7 @@ int kt_plant_cliques(uint32_t num_nodes, const uint32_t* u, const uint32_t* v, u
         return KT_ERR_INVALID_ARG;
     Rng rng(seed, 6);
     uint64_t ctr = 0;
-    std::vector<uint64_t> keys(num_edges);
-    for (uint64_t i = 0; i < num_edges; ++i) {
-        if (u[i] >= num_nodes || v[i] >= num_nodes) return KT_ERR_INVALID_ARG;
-        keys[i] = pack(u[i], v[i]);
-    }
+    std::vector<uint64_t> extra;
     std::vector<uint32_t> members;
     for (uint32_t q = 0; q < count; ++q) {
         uint32_t s = min_size + bounded(rng.at(ctr++), max_size - min_size + 1);
@@ -330,9 +326,48 @@ int kt_plant_cliques(uint32_t num_nodes, const uint32_t* u, const uint32_t* v, u
             if (std::find(members.begin(), members.end(), x) == members.end()) members.push_back(x);
         }
         for (size_t i = 0; i < members.size(); ++i)
-            for (size_t j = i + 1; j < members.size(); ++j) keys.push_back(pack(members[i], members[j]));
+            for (size_t j = i + 1; j < members.size(); ++j) extra.push_back(pack(members[i], members[j]));
     }
-    return finish(keys, num_nodes, out);
+    // Is the input canonical already (u < v, (u, v) strictly increasing, ids in range)?  Then only
+    // the clique edges are sorted and merged into it.
+    std::atomic<bool> canonical{true};
+    parallel_for(num_edges, [&](size_t lo, size_t hi) {
+        for (size_t i = lo; i < hi; ++i) {
+            if (u[i] >= v[i] || v[i] >= num_nodes || (i > 0 && pack(u[i - 1], v[i - 1]) >= pack(u[i], v[i]))) {
+                canonical = false;
+                return;
+            }
+        }
+    });
+    if (!canonical) {
+        std::vector<uint64_t> keys(num_edges);
+        for (uint64_t i = 0; i < num_edges; ++i) {
+            if (u[i] >= num_nodes || v[i] >= num_nodes) return KT_ERR_INVALID_ARG;
+            keys[i] = pack(u[i], v[i]);
+        }
+        keys.insert(keys.end(), extra.begin(), extra.end());
+        return finish(keys, num_nodes, out);
+    }
+    std::sort(extra.begin(), extra.end());
+    extra.erase(std::unique(extra.begin(), extra.end()), extra.end());
+    const uint64_t cap = num_edges + extra.size();
+    out->num_nodes = num_nodes;
+    out->u = (uint32_t*)malloc(sizeof(uint32_t) * (cap ? cap : 1));
+    out->v = (uint32_t*)malloc(sizeof(uint32_t) * (cap ? cap : 1));
+    if (!out->u || !out->v) { free(out->u); free(out->v); out->u = out->v = nullptr; return KT_ERR_HOST_ALLOC; }
+    uint64_t i = 0, j = 0, w = 0;
+    while (i < num_edges || j < extra.size()) {
+        const uint64_t a = i < num_edges ? pack(u[i], v[i]) : UINT64_MAX;
+        const uint64_t b = j < extra.size() ? extra[j] : UINT64_MAX;
+        const uint64_t k = a <= b ? a : b;
+        if (a <= b) ++i;
+        if (b <= a) ++j;
+        out->u[w] = (uint32_t)(k >> 32);
+        out->v[w] = (uint32_t)k;
+        ++w;
+    }
+    out->num_edges = w;
+    return KT_OK;
 }
 
 int kt_gen_batch(uint32_t num_graphs, uint32_t n_min, uint32_t n_max, uint64_t seed, kt_edges* out,

@@ -29,7 +29,8 @@ namespace {
 constexpr uint32_t kNoAllocMaxNodes = 1u << 17;       // 131,072 vertices
 constexpr uint64_t kNoAllocMaxEntries = 1ull << 19;   // 524,288 entries = 262,144 undirected edges
 constexpr size_t kNoAllocScratchBytes = 40ull << 20;  // 40 MiB, checked against the layout at set-up
-constexpr size_t kCtrlBytes = 256;                    // control words at the start of the array
+constexpr size_t kCtrlBytes = 512;                    // control words at the start of the array
+static_assert(kCtrlBytes >= sizeof(uint32_t) * kt::kCtrlWords, "control block does not fit");
 constexpr int kMaxDevices = 64;
 
 // File-scope scratch.  In host code this name is only a stand-in; its device address comes from

@@ -85,6 +85,8 @@ struct PeelParams {
     uint32_t cw_shift;  // log2 of the chunk width (row entries per work chunk): 3, 4 or 5
     uint32_t compact_num;  // rows are compacted once alive edges < compact_num/100 of the count
                            // at the last compaction (0: never)
+    uint32_t recount_num;  // a round whose frontier holds >= recount_num % of the alive edges
+                           // recounts the survivors' support instead of decrementing (0: never)
     uint32_t single_k;  // 0: full decomposition; >= 3: the k of a single-k truss
     uint64_t timeout_ns;
 };
@@ -122,16 +124,16 @@ __device__ __forceinline__ void push_edges(const PeelParams& P, uint32_t e, bool
         if (lane >= (uint32_t)o) incl += t;
     }
     const uint32_t total = __shfl_sync(kFullMask, incl, 31);
-    uint32_t cb = 0;
+    unsigned long long cb = 0;
     if (lane == 0) {
-        cb = atomicAdd(P.ctrl + kPNext + slot, total);
+        cb = atomicAdd(reinterpret_cast<unsigned long long*>(P.ctrl + kPChunks) + slot, (unsigned long long)total);
         atomicAdd(P.ctrl + kPEdges + slot, __popc(mt));
     }
     cb = __shfl_sync(kFullMask, cb, 0);
     uint4* ch = P.ch[rr & 1];
-    if ((uint64_t)cb + total <= P.cap_chunks) {
+    if (cb + total <= P.cap_chunks) {
         if (take) {
-            const uint32_t c0 = cb + incl - nch;
+            const uint32_t c0 = (uint32_t)cb + incl - nch;
             for (uint32_t c = 0; c < nch; ++c) {
                 const uint32_t off = c << P.cw_shift;
                 const uint32_t cnt = len > off ? min(1u << P.cw_shift, len - off) : 0u;
@@ -139,8 +141,8 @@ __device__ __forceinline__ void push_edges(const PeelParams& P, uint32_t e, bool
             }
         }
     } else {
-        const uint64_t stop = (uint64_t)cb + total < P.cap_chunks ? (uint64_t)cb + total : P.cap_chunks;
-        for (uint64_t i = (uint64_t)cb + lane; i < stop; i += 32) ch[i] = make_uint4(kNullChunk, 0, 0, 0);
+        const uint64_t stop = cb + total < P.cap_chunks ? cb + total : P.cap_chunks;
+        for (uint64_t i = cb + lane; i < stop; i += 32) ch[i] = make_uint4(kNullChunk, 0, 0, 0);
         uint32_t bb = 0;
         if (lane == 0) bb = atomicAdd(P.ctrl + kPBigCount + slot, __popc(mt));
         bb = __shfl_sync(kFullMask, bb, 0);
@@ -224,6 +226,48 @@ __device__ __forceinline__ void peel_entries(const PeelParams& P, uint32_t e, ui
         }
         push_edges(P, a[j], qa, r + 1);
         push_edges(P, b, qb, r + 1);
+    }
+}
+
+// Support of every alive edge (rnd == 0) counted again from scratch over the triangles whose
+// three edges are alive, for a round that removes most of the alive edges: walking the rows of
+// all removed edges would cost far more than counting what survives.  Supports of alive edges
+// must be zero on entry.  Groups of 8 lanes per oriented edge (u,v): the part of N+(u) above v
+// (it follows the edge in u's row) is intersected with N+(v), the shorter list walked and the
+// longer binary-searched, as in the support count; the oriented rows still hold removed edges,
+// which are skipped by their round stamps.
+__device__ void recount_support(const PeelParams& P, uint32_t start, uint64_t tid, uint64_t nthreads) {
+    constexpr uint32_t G = 8;
+    const uint32_t lane = lane_id(), glane = lane & (G - 1);
+    const uint32_t gmask = 0xffu << (lane & ~(G - 1));
+    for (uint64_t j64 = start + tid / G; j64 < P.m; j64 += nthreads / G) {
+        const uint32_t j = (uint32_t)j64;
+        if (P.rnd[j] != 0) continue;  // the same for the whole group
+        const uint32_t u = P.e_src[j], v = P.o_col[j];
+        const uint32_t a0 = j + 1, a1 = P.o_ptr[u + 1];
+        const uint32_t b0 = P.o_ptr[v], b1 = P.o_ptr[v + 1];
+        const uint32_t na = a1 - a0, nb = b1 - b0;
+        uint32_t cnt = 0;
+        if (na && nb) {
+            const bool iter_a = na <= nb;
+            const uint32_t i0 = iter_a ? a0 : b0, ni = iter_a ? na : nb;
+            const uint32_t s0 = iter_a ? b0 : a0, ns = iter_a ? nb : na;
+            for (uint32_t t = glane; t < ni; t += G) {
+                const uint32_t x = i0 + t;
+                if (P.rnd[x] != 0) continue;
+                const uint32_t w = __ldg(P.o_col + x);
+                const uint32_t y = s0 + lower_bound_u32(P.o_col + s0, ns, w);
+                if (y < s0 + ns && __ldg(P.o_col + y) == w && P.rnd[y] == 0) {
+                    ++cnt;
+                    atomicAdd(&P.sup[x], 1u);
+                    atomicAdd(&P.sup[y], 1u);
+                }
+            }
+        }
+        __syncwarp(gmask);
+#pragma unroll
+        for (int o = G / 2; o > 0; o >>= 1) cnt += __shfl_xor_sync(gmask, cnt, o);
+        if (glane == 0 && cnt) atomicAdd(&P.sup[j], cnt);
     }
 }
 
@@ -318,6 +362,7 @@ __device__ __forceinline__ void collect(const PeelParams& P, uint32_t thr, uint3
 __global__ void __launch_bounds__(kPeelThreads, 1) k_peel(PeelParams P) {
     __shared__ uint32_t warp_cnt[kPeelThreads / 32];
     uint32_t* ctrl = P.ctrl;
+    unsigned long long* chunk_ctr = reinterpret_cast<unsigned long long*>(ctrl + kPChunks);
     const uint32_t nblocks = gridDim.x;
     const uint32_t lane = lane_id();
     const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -363,7 +408,10 @@ __global__ void __launch_bounds__(kPeelThreads, 1) k_peel(PeelParams P) {
             if (leader) atomicOr(ctrl + kCtrlError, kErrRunaway);
             return;
         }
-        if (leader) ctrl[kPNext + ((rr + 1) & 3)] = ctrl[kPBigCount + ((rr + 1) & 3)] = ctrl[kPEdges + ((rr + 1) & 3)] = 0;
+        if (leader) {
+            chunk_ctr[(rr + 1) & 3] = 0;
+            ctrl[kPBigCount + ((rr + 1) & 3)] = ctrl[kPEdges + ((rr + 1) & 3)] = 0;
+        }
         // compact the rows once the alive edges have dropped enough since the last compaction
         if (live * 100 < live_at_compaction * P.compact_num) {
             compact_rows(P, r, warp_cnt);
@@ -372,6 +420,7 @@ __global__ void __launch_bounds__(kPeelThreads, 1) k_peel(PeelParams P) {
             ++compactions;
             live_at_compaction = live;
         }
+        uint32_t lvl_start = 0;  // no edge below this id is alive at this level
         if (P.single_k == 0) {
             // one pass over the alive list: compact it, minimum support, and the frontier of
             // level k_last+1 (the usual next level); a second pass only if that level is empty
@@ -426,8 +475,9 @@ __global__ void __launch_bounds__(kPeelThreads, 1) k_peel(PeelParams P) {
             KT_PHASE(1)
             if (ld_acquire(ctrl + kPLAlive + ls) == 0) break;
             k = ld_acquire(ctrl + kPLMin + ls) + 3;
+            lvl_start = ld_acquire(ctrl + kPLMinId + ls);
             if (k != kg) {
-                collect(P, k - 3, rr, ld_acquire(ctrl + kPLMinId + ls), tid, nthreads);
+                collect(P, k - 3, rr, lvl_start, tid, nthreads);
                 if (!grid_barrier(ctrl, nblocks, P.timeout_ns)) return;
                 KT_PHASE(2)
             }
@@ -445,7 +495,7 @@ __global__ void __launch_bounds__(kPeelThreads, 1) k_peel(PeelParams P) {
             P.level_ns[level] = (uint32_t)(global_ns() - level_t0);
             P.level_front[level] = E;
         }
-        uint32_t C = min(ld_acquire(ctrl + kPNext + (rr & 3)), P.cap_chunks);
+        uint32_t C = (uint32_t)min(ld_acquire_u64(chunk_ctr + (rr & 3)), (unsigned long long)P.cap_chunks);
         while (E) {
             ++r;
             ++rounds;
@@ -455,7 +505,7 @@ __global__ void __launch_bounds__(kPeelThreads, 1) k_peel(PeelParams P) {
             }
             if (leader) {
                 const uint32_t z = (r + 2) & 3;
-                ctrl[kPNext + z] = 0;
+                chunk_ctr[z] = 0;
                 ctrl[kPBigCount + z] = 0;
                 ctrl[kPEdges + z] = 0;
                 if (rounds < P.cap_rounds) {
@@ -463,6 +513,27 @@ __global__ void __launch_bounds__(kPeelThreads, 1) k_peel(PeelParams P) {
                     P.round_level[rounds] = k;
                 }
             }
+            const bool recount = P.recount_num != 0 && (uint64_t)E * 100 >= (uint64_t)P.recount_num * live;
+            const unsigned long long round_t0 = leader ? phase_ns[6] : 0ull;
+            if (recount) {
+                // the whole frontier is removed at once (truss number k-1), the support of every
+                // surviving edge is counted again, and the next frontier comes from a scan
+                for (uint64_t j = lvl_start + tid; j < P.m; j += nthreads) {
+                    const uint32_t st = P.rnd[j];
+                    if (st == r) {
+                        P.tr[j] = k - 1;
+                        P.sup[j] = kDead;
+                    } else if (st == 0) {
+                        P.sup[j] = 0;
+                    }
+                }
+                if (!grid_barrier(ctrl, nblocks, P.timeout_ns)) return;
+                KT_PHASE(4)
+                recount_support(P, lvl_start, tid, nthreads);
+                if (!grid_barrier(ctrl, nblocks, P.timeout_ns)) return;
+                KT_PHASE(4)
+                collect(P, k - 3, r + 1, lvl_start, tid, nthreads);
+            } else {
             // chunks: a warp takes 32 / W chunks at a time, W lanes per chunk of up to W row
             // entries
             {
@@ -512,13 +583,14 @@ __global__ void __launch_bounds__(kPeelThreads, 1) k_peel(PeelParams P) {
                         peel_entries<1>(P, e, y, base, len, t0, lane, parts * blockDim.x, r, km2);
                 }
             }
+            }
             if (!grid_barrier(ctrl, nblocks, P.timeout_ns)) return;
-            if (leader && rounds < P.cap_rounds) P.round_ns[rounds] = (uint32_t)(global_ns() - phase_ns[6]);
-            KT_PHASE(5)
+            if (leader && rounds < P.cap_rounds) P.round_ns[rounds] = (uint32_t)(global_ns() - round_t0);
+            KT_PHASE(recount ? 4 : 5)
             live -= E;
             E = ld_acquire(ctrl + kPEdges + ((r + 1) & 3));
             B = ld_acquire(ctrl + kPBigCount + ((r + 1) & 3));
-            C = min(ld_acquire(ctrl + kPNext + ((r + 1) & 3)), P.cap_chunks);
+            C = (uint32_t)min(ld_acquire_u64(chunk_ctr + ((r + 1) & 3)), (unsigned long long)P.cap_chunks);
         }
         ++level;
         k_last = k;
@@ -653,6 +725,7 @@ int launch_peel(kt_engine* e, uint32_t single_k) {
     P.big_row = e->big_row;
     P.cw_shift = e->sched.chunk_width == 8 ? 3u : e->sched.chunk_width == 16 ? 4u : 5u;
     P.compact_num = e->sched.compact_percent;
+    P.recount_num = e->sched.recount_percent;
     P.single_k = single_k;
     P.timeout_ns = kPeelTimeoutNs;
     void* args[] = {&P};

@@ -79,16 +79,19 @@ class Stats(ctypes.Structure):
 
 
 class Schedule(ctypes.Structure):
-    """kt_schedule: lanes per edge of the support count, row entries per peel chunk, and the
-    alive-edge percentage below which rows are compacted (0 = never).  Results never depend on it."""
+    """kt_schedule: lanes per edge of the support count, row entries per peel chunk, the
+    alive-edge percentage below which rows are compacted (0 = never), and the frontier share of
+    the alive edges from which a round recounts the survivors instead of decrementing (0 = never).
+    Results never depend on it."""
     _fields_ = [("support_group", ctypes.c_uint32), ("chunk_width", ctypes.c_uint32),
-                ("compact_percent", ctypes.c_uint32)]
+                ("compact_percent", ctypes.c_uint32), ("recount_percent", ctypes.c_uint32)]
 
     def as_tuple(self) -> tuple:
-        return (self.support_group, self.chunk_width, self.compact_percent)
+        return (self.support_group, self.chunk_width, self.compact_percent, self.recount_percent)
 
     def __repr__(self) -> str:
-        return "Schedule(support_group=%d, chunk_width=%d, compact_percent=%d)" % self.as_tuple()
+        return ("Schedule(support_group=%d, chunk_width=%d, compact_percent=%d, recount_percent=%d)"
+                % self.as_tuple())
 
 
 _LIB = None
@@ -363,8 +366,9 @@ class Engine:
         _check(lib().kt_engine_ktruss(self._h, d_src, d_dst, num_entries, num_nodes, k & 0xFFFFFFFF, d_keep,
                                       int(sync)))
 
-    def set_schedule(self, support_group: int = 8, chunk_width: int = 32, compact_percent: int = 85) -> None:
-        s = Schedule(support_group, chunk_width, compact_percent)
+    def set_schedule(self, support_group: int = 8, chunk_width: int = 32, compact_percent: int = 85,
+                     recount_percent: int = 0) -> None:
+        s = Schedule(support_group, chunk_width, compact_percent, recount_percent)
         _check(lib().kt_engine_set_schedule(self._h, ctypes.byref(s)))
 
     def schedule(self) -> Schedule:
@@ -416,9 +420,10 @@ def schedule_default() -> Schedule:
     return lib().kt_schedule_default()
 
 
-def set_schedule(support_group: int = 8, chunk_width: int = 32, compact_percent: int = 85) -> None:
+def set_schedule(support_group: int = 8, chunk_width: int = 32, compact_percent: int = 85,
+                 recount_percent: int = 0) -> None:
     """Schedule of the engine behind the host-buffer calls (ktruss, decompose, decompose_batch)."""
-    s = Schedule(support_group, chunk_width, compact_percent)
+    s = Schedule(support_group, chunk_width, compact_percent, recount_percent)
     _check(lib().kt_set_schedule(ctypes.byref(s)))
 
 

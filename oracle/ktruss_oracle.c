@@ -87,13 +87,35 @@ typedef struct {
     uint32_t* edge_affected;
 } info_t; /* Info, info.h:14-19 */
 
+/* Optional wall-clock deadline for ko_chain_sample (0 = none); checked between passes and every
+ * 4096 edges of a directed count.  When a count is cut, g_cut_alive holds the alive edges it had
+ * merged. */
+static double g_deadline = 0.0;
+static int g_deadline_hit = 0;
+static int g_cut_in_count = 0;
+static uint64_t g_cut_alive = 0;
+
+static double now_s(void) {
+    struct timespec ts;
+    clock_gettime(CLOCK_MONOTONIC, &ts);
+    return (double)ts.tv_sec + 1e-9 * (double)ts.tv_nsec;
+}
+
 /* count_triangles, directed CSR (kernel_hdc.cu:11-49): merge of the two sorted out-lists,
  * each match credits the edge and both other edges of the triangle. */
 static void count_directed(csr_t* g, info_t* in, int check_deleted, int recount_all) {
+    uint64_t merged = 0;
     for (uint32_t e = 0; e < g->num_edges; ++e) {
+        if (g_deadline > 0.0 && (e & 4095u) == 0 && now_s() > g_deadline) {
+            g_deadline_hit = 1;
+            g_cut_in_count = 1;
+            g_cut_alive = merged;
+            return;
+        }
         if (!(recount_all || in->edge_affected[e] == DIRECTLY_AFFECTED || in->edge_affected[e] == INDIRECTLY_AFFECTED)) continue;
         uint32_t dst = g->dst[e];
         if (check_deleted && dst == KO_DELETED) continue;
+        ++merged;
         uint32_t e1 = g->ptr[g->src[e]], end1 = g->ptr[g->src[e] + 1];
         uint32_t e2 = g->ptr[dst], end2 = g->ptr[dst + 1];
         while (e1 < end1 && e2 < end2) {
@@ -190,16 +212,6 @@ static uint64_t alive_edges(const csr_t* g) {
     return c;
 }
 
-/* Optional wall-clock deadline for ko_chain_sample (0 = none); checked between passes. */
-static double g_deadline = 0.0;
-static int g_deadline_hit = 0;
-
-static double now_s(void) {
-    struct timespec ts;
-    clock_gettime(CLOCK_MONOTONIC, &ts);
-    return (double)ts.tv_sec + 1e-9 * (double)ts.tv_nsec;
-}
-
 /* The peel loop shared by kernel_hdc.cu:107-201 and kernel_huc.cu:87-179. */
 static void peel_loop(csr_t* g, uint32_t k, int directed, int recount, uint32_t num_edge_remove_iter,
                       info_t* in, uint32_t num_slots, ko_pass_log* log) {
@@ -222,6 +234,7 @@ static void peel_loop(csr_t* g, uint32_t k, int directed, int recount, uint32_t 
         }
         if (directed) count_directed(g, in, has_deleted, all);
         else count_undirected(g, k, in, has_deleted, all);
+        if (g_deadline_hit) break; /* a count cut by the deadline: the pass is abandoned */
         mark_deleted(g, k, in, has_deleted, all);
         changed = in->changed;
         if (changed) {
@@ -402,11 +415,18 @@ int ko_chain_sample(uint32_t num_nodes, uint32_t num_entries, const uint32_t* sr
     log.alive = alive;
     g_deadline = t0 + budget_s;
     g_deadline_hit = 0;
+    g_cut_in_count = 0;
+    g_cut_alive = 0;
     for (uint32_t k = 3; cur > 0 && !g_deadline_hit; ++k) {
         uint32_t nout = 0;
         if (ko_ktruss(num_nodes, cur, cs, cd, k, KO_DIRECTED_BY_DEGREE, KO_RECOUNT_ALL, 0, os, od, &nout, &log)) goto done;
-        /* a pass cut by the deadline is not counted (log.num counts started passes) */
+        /* a pass cut by the deadline counts only the alive edges its count had merged
+         * (log.num counts started passes) */
         uint32_t full = log.num;
+        if (g_cut_in_count && full > 0) {
+            --full;
+            alive_sum += g_cut_alive;
+        }
         for (uint32_t p = 0; p < full && p < log.cap; ++p) alive_sum += log.alive[p];
         passes += full;
         if (nout == 0) break;

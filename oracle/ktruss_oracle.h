@@ -50,8 +50,9 @@ int ko_decompose_chain(uint32_t num_nodes, uint32_t num_entries, const uint32_t*
                        uint32_t* plain_passes, uint64_t* plain_alive_sum);
 
 /* Bounded sample of ko_decompose_chain for CPU timing: runs the chain's count-and-prune passes
- * in order and stops at the first pass boundary after `budget_s` seconds.  Reports the passes
- * done, the sum of their alive oriented edge counts and the elapsed seconds. */
+ * in order and stops once `budget_s` seconds have passed (at a pass boundary, or inside a
+ * pass's triangle count).  Reports the complete passes, the alive oriented edges they visited
+ * plus those the cut count had merged, and the elapsed seconds. */
 int ko_chain_sample(uint32_t num_nodes, uint32_t num_entries, const uint32_t* src, const uint32_t* dst,
                     double budget_s, uint32_t* passes_done, uint64_t* alive_done, double* seconds);
 

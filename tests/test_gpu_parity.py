@@ -57,6 +57,8 @@ GENERATED = [
     ("ws20000", lambda: kt.gen_ws(20000, 20, 0.1, 6)),
     ("rgg20000", lambda: kt.gen_rgg(20000, 0.02, 7)),
     ("er8192_cliques", lambda: kt.plant_cliques(*kt.gen_er(8192, 0.002, 8), 4, 30, 90, 10)),
+    # the stress family (edge factor 32, 64-512 cliques) at a size the oracle finishes
+    ("rmat15_ef32_cliques", lambda: kt.plant_cliques(*kt.gen_rmat(15, 32, 0.57, 0.19, 0.19, 1), 4, 64, 200, 8)),
 ]
 
 

@@ -17,7 +17,7 @@ GRAPHS = [
     ("ws8000", lambda: kt.gen_ws(8000, 10, 0.1, 14)),
 ]
 
-SCHEDULES = list(itertools.product((4, 8, 16, 32), (8, 16, 32), (0, 50, 85)))
+SCHEDULES = list(itertools.product((4, 8, 16, 32), (8, 16, 32), (0, 50, 85), (0, 1, 50)))
 
 
 @pytest.fixture(scope="module")
@@ -35,25 +35,25 @@ def test_every_schedule_matches_oracle(name, make, torch):
     d_dst = torch.from_numpy(dst.view(np.int32)).cuda()
     d_out = torch.empty(len(src), dtype=torch.int32, device="cuda")
     d_k = torch.zeros(1, dtype=torch.int32, device="cuda")
-    for g, w, c in SCHEDULES:
-        eng.set_schedule(g, w, c)
-        assert eng.schedule().as_tuple() == (g, w, c)
+    for g, w, c, rc in SCHEDULES:
+        eng.set_schedule(g, w, c, rc)
+        assert eng.schedule().as_tuple() == (g, w, c, rc)
         d_out.fill_(-1)
         torch.cuda.synchronize()  # the engine runs on its own stream
         eng.decompose(d_src.data_ptr(), d_dst.data_ptr(), len(src), n, d_out.data_ptr(), d_k.data_ptr())
-        assert int(d_k.item()) == ref["k_max"], (g, w, c)
-        assert np.array_equal(d_out.cpu().numpy().view(np.uint32), ref["truss"]), (g, w, c)
+        assert int(d_k.item()) == ref["k_max"], (g, w, c, rc)
+        assert np.array_equal(d_out.cpu().numpy().view(np.uint32), ref["truss"]), (g, w, c, rc)
         st = eng.stats()
         assert st.compactions == 0 or c != 0
 
 
-@pytest.mark.parametrize("w", [8, 16])
-def test_single_k_with_narrow_chunks(w, torch):
+@pytest.mark.parametrize("w,rc", [(8, 0), (16, 0), (32, 50), (8, 1)])
+def test_single_k_with_narrow_chunks(w, rc, torch):
     n, u, v = kt.plant_cliques(*kt.gen_ba(5000, 8, 21), 2, 20, 40, 22)
     src, dst = both_directions(u, v)
     ref = oracle.decompose(n, src, dst, method="peel")
     eng = kt.Engine(0)
-    eng.set_schedule(16, w, 85)
+    eng.set_schedule(16, w, 85, rc)
     d_src = torch.from_numpy(src.view(np.int32)).cuda()
     d_dst = torch.from_numpy(dst.view(np.int32)).cuda()
     keep = torch.empty(len(src), dtype=torch.uint8, device="cuda")
@@ -67,7 +67,7 @@ def test_batch_with_narrow_chunks(torch):
     n, u, v, off = kt.gen_batch(24, 500, 4000, 31)
     src, dst = both_directions(u, v)
     eng = kt.Engine(0)
-    eng.set_schedule(4, 8, 50)
+    eng.set_schedule(4, 8, 50, 25)
     d_src = torch.from_numpy(src.view(np.int32)).cuda()
     d_dst = torch.from_numpy(dst.view(np.int32)).cuda()
     d_off = torch.from_numpy(off.view(np.int32)).cuda()
@@ -80,7 +80,8 @@ def test_batch_with_narrow_chunks(torch):
     assert np.array_equal(d_out.cpu().numpy().view(np.uint32), ref["truss"])
 
 
-@pytest.mark.parametrize("bad", [(2, 32, 85), (64, 32, 85), (8, 4, 85), (8, 64, 85), (8, 32, 100)])
+@pytest.mark.parametrize("bad", [(2, 32, 85, 0), (64, 32, 85, 0), (8, 4, 85, 0), (8, 64, 85, 0), (8, 32, 100, 0),
+                                 (8, 32, 85, 101)])
 def test_invalid_schedule_rejected(bad):
     eng = kt.Engine(0)
     before = eng.schedule().as_tuple()
@@ -101,8 +102,8 @@ def _clique_union(sizes):
 
 
 @pytest.mark.parametrize("sizes", [[20] * 300, [100, 100, 64]], ids=["many_small", "few_large"])
-@pytest.mark.parametrize("w", [8, 32])
-def test_chunk_buffer_overflow(sizes, w, torch):
+@pytest.mark.parametrize("w,rc", [(8, 0), (32, 0), (8, 50)])
+def test_chunk_buffer_overflow(sizes, w, rc, torch):
     """A level whose whole frontier is every edge of many cliques needs more chunks than the
     buffer holds (m + 4096 on an engine sized for this graph): the rest is walked by warps (many
     edges) or blocks (few edges).  Every edge of a c-clique has truss number c."""
@@ -115,7 +116,7 @@ def test_chunk_buffer_overflow(sizes, w, torch):
     expect = np.concatenate([np.full(s * (s - 1) // 2, s, np.uint32) for s in sizes])
     eng = kt.Engine(0)
     eng.reserve(n, len(src))
-    eng.set_schedule(8, w, 85)
+    eng.set_schedule(8, w, 85, rc)
     d_src = torch.from_numpy(src.view(np.int32)).cuda()
     d_dst = torch.from_numpy(dst.view(np.int32)).cuda()
     d_out = torch.empty(len(src), dtype=torch.int32, device="cuda")
