@@ -191,7 +191,7 @@ typedef struct kt_schedule {
                                   (its affected-edge recount, made exact): 1..100, or 0 = never */
 } kt_schedule;
 
-/* The default schedule {8, 32, 85, 0}. */
+/* The default schedule {8, 32, 85, 50}. */
 kt_schedule kt_schedule_default(void);
 
 /* Creates an engine on `device` with its own non-blocking CUDA stream. */

@@ -300,7 +300,7 @@ int kt_engine_ktruss(kt_engine* e, const uint32_t* d_src, const uint32_t* d_dst,
     return KT_OK;
 }
 
-kt_schedule kt_schedule_default(void) { return kt_schedule{8, 32, 85, 0}; }
+kt_schedule kt_schedule_default(void) { return kt_schedule{8, 32, 85, 50}; }
 
 int kt_engine_set_schedule(kt_engine* e, const kt_schedule* s) {
     kt::clear_error();

@@ -84,7 +84,7 @@ struct kt_engine {
     uint32_t m = 0;
     uint32_t vb = 1;  // bits per rank in sort keys
 
-    kt_schedule sched{8, 32, 85, 0};  // kernel schedule (kt_engine_set_schedule)
+    kt_schedule sched{8, 32, 85, 50};  // kernel schedule (kt_engine_set_schedule)
     kt_stats stats{};
     int peel_mode = 0;          // 0 decomposition, 1 single-k
     bool stats_ready = false;   // stats already read back from the device

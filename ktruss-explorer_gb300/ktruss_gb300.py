@@ -367,7 +367,7 @@ class Engine:
                                       int(sync)))
 
     def set_schedule(self, support_group: int = 8, chunk_width: int = 32, compact_percent: int = 85,
-                     recount_percent: int = 0) -> None:
+                     recount_percent: int = 50) -> None:
         s = Schedule(support_group, chunk_width, compact_percent, recount_percent)
         _check(lib().kt_engine_set_schedule(self._h, ctypes.byref(s)))
 
@@ -421,7 +421,7 @@ def schedule_default() -> Schedule:
 
 
 def set_schedule(support_group: int = 8, chunk_width: int = 32, compact_percent: int = 85,
-                 recount_percent: int = 0) -> None:
+                 recount_percent: int = 50) -> None:
     """Schedule of the engine behind the host-buffer calls (ktruss, decompose, decompose_batch)."""
     s = Schedule(support_group, chunk_width, compact_percent, recount_percent)
     _check(lib().kt_set_schedule(ctypes.byref(s)))
