@@ -262,6 +262,46 @@ uint32_t kt_schedule_grid(kt_schedule* out, uint32_t cap);
 int kt_engine_autotune(kt_engine* engine, const uint32_t* d_src, const uint32_t* d_dst, uint64_t num_entries,
                        uint32_t num_nodes, const kt_schedule* candidates, uint32_t num_candidates,
                        uint32_t repeats, float* ms, kt_schedule* best);
+/* ---- learned schedule selector (no counterpart in the reference) ------------------------
+ * A small MLP (16 -> 64 -> 64 -> 19, ReLU, FP32, hand-written CUDA kernels for inference,
+ * training and Adam) that reads 16 statistics of a built graph and predicts its schedule from
+ * the autotuner's grid: the variant (support_group x chunk_width x compact_percent, 18 classes)
+ * and the recount switch (recount_percent 50 or 0).  It is trained on timings of the grid's 36
+ * schedules (kt_engine_autotune with ms output) measured on graphs like the ones it will see.
+ * Every schedule gives the same truss numbers: a wrong prediction only costs time. */
+#define KT_SELECTOR_FEATURES 16
+#define KT_SELECTOR_VARIANTS 18
+#define KT_SELECTOR_SCHEDULES 36
+#define KT_SELECTOR_PARAMS 6483
+typedef struct kt_selector kt_selector;
+/* A selector on `device` with seeded He-uniform weights and identity standardization. */
+int kt_selector_create(int device, uint64_t seed, kt_selector** out);
+int kt_selector_destroy(kt_selector* selector);
+/* Parameters (KT_SELECTOR_PARAMS floats: W1[64][16], b1[64], W2[64][64], b2[64], W3[19][64],
+ * b3[19]) and the input standardization (mean, scale: 16 floats each); any pointer may be NULL. */
+int kt_selector_get_params(kt_selector* selector, float* params, float* mean, float* scale);
+int kt_selector_set_params(kt_selector* selector, const float* params, const float* mean, const float* scale);
+/* Trains on n graphs: features (n x 16, as kt_engine_features gives them) and times (n x 36 ms in
+ * kt_schedule_grid order).  Sets the standardization from these features, then runs `epochs` of
+ * Adam (learning rate lr) over minibatches of `batch` graphs in a seeded order.  Loss per graph:
+ * softmax cross-entropy of the best variant plus the logistic loss of the recount switch.
+ * epoch_loss (optional): mean loss of each epoch. */
+int kt_selector_train(kt_selector* selector, const float* features, const float* times, uint32_t n, uint32_t epochs,
+                      uint32_t batch, float lr, uint64_t seed, float* epoch_loss);
+/* Mean loss and its gradient (KT_SELECTOR_PARAMS floats, optional) over all n graphs at the
+ * current parameters and standardization. */
+int kt_selector_gradient(kt_selector* selector, const float* features, const float* times, uint32_t n, float* grad,
+                         float* loss);
+/* Predicted schedules of n graphs from their features. */
+int kt_selector_predict(kt_selector* selector, const float* features, uint32_t n, kt_schedule* out);
+/* Builds the graph and returns its 16 features (computed on the device). */
+int kt_engine_features(kt_engine* engine, const uint32_t* d_src, const uint32_t* d_dst, uint64_t num_entries,
+                       uint32_t num_nodes, float* features);
+/* With a selector attached, every decomposition (single graph or batch) computes the features
+ * of the built graph, runs the network on the device and uses its schedule (the call then waits
+ * for the build before it enqueues the rest); NULL detaches it and keeps the last schedule. */
+int kt_engine_set_selector(kt_engine* engine, kt_selector* selector);
+
 /* Self-test of the bounded device waits: launches a grid barrier that one block never reaches,
  * with a wait limit of timeout_ns (at most 5 s).  Returns KT_ERR_TIMEOUT when the wait expired
  * and the kernel returned as designed; the engine stays usable afterwards. */

@@ -83,6 +83,9 @@ size_t carve(kt_engine* e, char* base, uint32_t n, uint64_t N, bool staging) {
     e->level_alive = c.take<uint32_t>(e->cap_levels);
     e->level_ns = c.take<uint32_t>(e->cap_levels);
     e->level_front = c.take<uint32_t>(e->cap_levels);
+    e->sel_stats = c.take<uint32_t>(32);
+    e->sel_feat = c.take<float>(KT_SELECTOR_FEATURES);
+    e->sel_choice = c.take<uint32_t>(1);
     e->hist = c.take<uint32_t>(hist_words);
     e->hist_words = hist_words;
     e->scan_tmp = c.take<uint32_t>(scan_words);
@@ -181,6 +184,7 @@ int run_decompose(kt_engine* e, const uint32_t* d_src, const uint32_t* d_dst, ui
     int rc;
     if ((rc = record_start(e))) return rc;
     if ((rc = kt::build_graph(e, d_src, d_dst, entries, n))) return rc;
+    if ((rc = kt::select_schedule(e))) return rc;
     if ((rc = record(e, e->ev_built))) return rc;
     if ((rc = kt::count_support(e))) return rc;
     if ((rc = record(e, e->ev_counted))) return rc;
@@ -400,6 +404,27 @@ int kt_engine_autotune(kt_engine* e, const uint32_t* d_src, const uint32_t* d_ds
     e->sched = candidates[best_i];
     if (best) *best = candidates[best_i];
     return KT_OK;
+}
+
+int kt_engine_set_selector(kt_engine* e, kt_selector* s) {
+    kt::clear_error();
+    if (!e) return fail(KT_ERR_INVALID_ARG, "kt_engine_set_selector: null engine");
+    e->selector = s;
+    return KT_OK;
+}
+
+int kt_engine_features(kt_engine* e, const uint32_t* d_src, const uint32_t* d_dst, uint64_t num_entries,
+                       uint32_t num_nodes, float* features) {
+    kt::clear_error();
+    if (!e || !features) return fail(KT_ERR_INVALID_ARG, "kt_engine_features: null argument");
+    if (num_entries && (!d_src || !d_dst)) return fail(KT_ERR_INVALID_ARG, "kt_engine_features: null buffer");
+    int rc = check_cuda(cudaSetDevice(e->device), "cudaSetDevice");
+    if (rc || (rc = kt::build_graph(e, d_src, d_dst, num_entries, num_nodes)) ||
+        (rc = kt::graph_features(e, nullptr)) ||
+        (rc = check_cuda(cudaMemcpyAsync(features, e->sel_feat, sizeof(float) * KT_SELECTOR_FEATURES,
+                                         cudaMemcpyDeviceToHost, e->stream), "read features")))
+        return rc;
+    return check_cuda(cudaStreamSynchronize(e->stream), "synchronize");
 }
 
 int kt_engine_selftest_barrier_timeout(kt_engine* e, uint64_t timeout_ns) {

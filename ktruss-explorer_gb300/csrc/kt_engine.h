@@ -85,6 +85,10 @@ struct kt_engine {
     uint32_t vb = 1;  // bits per rank in sort keys
 
     kt_schedule sched{8, 32, 85, 50};  // kernel schedule (kt_engine_set_schedule)
+    kt_selector* selector = nullptr;   // learned schedule selector (kt_engine_set_selector)
+    uint32_t* sel_stats = nullptr;     // 16 u64 graph statistics for the selector's features
+    float* sel_feat = nullptr;         // the 16 features
+    uint32_t* sel_choice = nullptr;    // the selector's schedule index
     kt_stats stats{};
     int peel_mode = 0;          // 0 decomposition, 1 single-k
     bool stats_ready = false;   // stats already read back from the device
@@ -121,6 +125,11 @@ int emit_truss_per_entry(kt_engine* e, uint32_t* d_out, uint32_t* d_k_max);
 int emit_keep(kt_engine* e, uint8_t* d_keep);
 int emit_graph_kmax(kt_engine* e, const uint32_t* d_src, const uint32_t* d_dst, const uint32_t* d_offsets,
                     uint32_t num_graphs, const uint32_t* d_truss, uint32_t* d_kmax);
+// kt_selector.cu: graph statistics and features of the built graph into e->sel_feat (and, with
+// d_params, the selector's schedule index into e->sel_choice); select_schedule applies the
+// attached selector's choice to e->sched.
+int graph_features(kt_engine* e, const float* d_params);
+int select_schedule(kt_engine* e);
 // Reads the peel's control block and round log (stream must be drained); reports timeouts.
 int finish_stats(kt_engine* e);
 // Launches a grid barrier that cannot complete and returns the status it reports.

@@ -144,6 +144,17 @@ def lib() -> ctypes.CDLL:
         L.kt_schedule_default.argtypes = []
         L.kt_engine_set_schedule.argtypes = [_VP, ctypes.POINTER(Schedule)]
         L.kt_engine_get_schedule.argtypes = [_VP, ctypes.POINTER(Schedule)]
+        _FP = ctypes.POINTER(ctypes.c_float)
+        L.kt_selector_create.argtypes = [ctypes.c_int, ctypes.c_uint64, ctypes.POINTER(_VP)]
+        L.kt_selector_destroy.argtypes = [_VP]
+        L.kt_selector_get_params.argtypes = [_VP, _FP, _FP, _FP]
+        L.kt_selector_set_params.argtypes = [_VP, _FP, _FP, _FP]
+        L.kt_selector_train.argtypes = [_VP, _FP, _FP, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
+                                        ctypes.c_float, ctypes.c_uint64, _FP]
+        L.kt_selector_gradient.argtypes = [_VP, _FP, _FP, ctypes.c_uint32, _FP, _FP]
+        L.kt_selector_predict.argtypes = [_VP, _FP, ctypes.c_uint32, ctypes.POINTER(Schedule)]
+        L.kt_engine_features.argtypes = [_VP, _VP, _VP, ctypes.c_uint64, ctypes.c_uint32, _FP]
+        L.kt_engine_set_selector.argtypes = [_VP, _VP]
         L.kt_set_schedule.argtypes = [ctypes.POINTER(Schedule)]
         L.kt_get_schedule.argtypes = [ctypes.POINTER(Schedule)]
         L.kt_schedule_grid.argtypes = [ctypes.POINTER(Schedule), ctypes.c_uint32]
@@ -389,6 +400,17 @@ class Engine:
                                         ctypes.byref(best)))
         return best, [(arr[i], ms[i]) for i in range(len(cands))]
 
+    def features(self, d_src: int, d_dst: int, num_entries: int, num_nodes: int) -> np.ndarray:
+        """The selector's 16 features of this device graph (built on the device)."""
+        out = np.zeros(SELECTOR_FEATURES, np.float32)
+        _check(lib().kt_engine_features(self._h, d_src, d_dst, num_entries, num_nodes, _fp(out)))
+        return out
+
+    def set_selector(self, selector: Optional["Selector"]) -> None:
+        """Attach a learned selector (its schedule is used by every decomposition) or detach (None)."""
+        self._selector = selector  # keep it alive while attached
+        _check(lib().kt_engine_set_selector(self._h, selector._h if selector is not None else None))
+
     def selftest_barrier_timeout(self, timeout_ns: int) -> int:
         """Status of a grid barrier that cannot complete (KT_ERR_TIMEOUT = 11 when correct)."""
         return lib().kt_engine_selftest_barrier_timeout(self._h, timeout_ns)
@@ -414,6 +436,76 @@ class Engine:
         s = Stats()
         _check(lib().kt_engine_stats(self._h, ctypes.byref(s)))
         return s
+
+
+SELECTOR_FEATURES, SELECTOR_VARIANTS, SELECTOR_SCHEDULES, SELECTOR_PARAMS = 16, 18, 36, 6483
+
+
+def _fp(a: Optional[np.ndarray]):
+    return None if a is None else a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+
+
+def _f32(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+class Selector:
+    """Learned schedule selector (kt_selector): FP32 MLP 16-64-64-19 trained and run by the
+    library's own CUDA kernels."""
+
+    def __init__(self, device: int = 0, seed: int = 1):
+        h = _VP()
+        _check(lib().kt_selector_create(device, seed, ctypes.byref(h)))
+        self._h = h
+
+    def close(self) -> None:
+        if self._h:
+            lib().kt_selector_destroy(self._h)
+            self._h = _VP()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def params(self) -> tuple:
+        p = np.zeros(SELECTOR_PARAMS, np.float32)
+        mean = np.zeros(SELECTOR_FEATURES, np.float32)
+        scale = np.zeros(SELECTOR_FEATURES, np.float32)
+        _check(lib().kt_selector_get_params(self._h, _fp(p), _fp(mean), _fp(scale)))
+        return p, mean, scale
+
+    def set_params(self, params=None, mean=None, scale=None) -> None:
+        a = [None if x is None else _f32(x) for x in (params, mean, scale)]
+        _check(lib().kt_selector_set_params(self._h, *[_fp(x) for x in a]))
+
+    def train(self, features, times, epochs: int = 200, batch: int = 64, lr: float = 3e-3, seed: int = 1):
+        """Trains on (n x 16 features, n x 36 times in ms); returns the mean loss of each epoch."""
+        f, t = _f32(features), _f32(times)
+        assert f.shape[1] == SELECTOR_FEATURES and t.shape == (f.shape[0], SELECTOR_SCHEDULES)
+        losses = np.zeros(epochs, np.float32)
+        _check(lib().kt_selector_train(self._h, _fp(f), _fp(t), f.shape[0], epochs, batch, lr, seed, _fp(losses)))
+        return losses
+
+    def gradient(self, features, times) -> tuple:
+        f, t = _f32(features), _f32(times)
+        g = np.zeros(SELECTOR_PARAMS, np.float32)
+        loss = ctypes.c_float(0)
+        _check(lib().kt_selector_gradient(self._h, _fp(f), _fp(t), f.shape[0], _fp(g), ctypes.byref(loss)))
+        return loss.value, g
+
+    def predict(self, features) -> list:
+        f = _f32(features).reshape(-1, SELECTOR_FEATURES)
+        out = (Schedule * max(1, f.shape[0]))()
+        _check(lib().kt_selector_predict(self._h, _fp(f), f.shape[0], out))
+        return [out[i] for i in range(f.shape[0])]
+
+
+def schedule_index(s) -> int:
+    """Position of a schedule in the autotuner's grid."""
+    t = s.as_tuple() if isinstance(s, Schedule) else tuple(s)
+    return [g.as_tuple() for g in schedule_grid()].index(t)
 
 
 def schedule_default() -> Schedule:
