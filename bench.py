@@ -186,6 +186,10 @@ def cpu_sample(n, src, dst, budget_s, pass_volume):
 def run_reference(args, world, rank):
     if rank != 0:
         return
+    if args.workload not in WORKLOADS:
+        print(json.dumps({"impl": "reference", "unavailable": "the reference CPU arm is timed on the single-graph "
+                                                              "workloads (the reference has no batch or selector)"}))
+        return
     n, m, src, dst = make_graph(args.workload)
     vol = PASS_VOLUME.get(args.workload)
     # untimed warm-up on a small graph (the sample's first pass alone is the full-graph count)
@@ -225,19 +229,40 @@ def run_reference(args, world, rank):
 def parse_schedule(text):
     """'default', 'auto' or 'G,W,C,R' (support group, chunk width, compaction percent, recount
     percent)."""
-    if text in ("default", "auto"):
+    if text in ("default", "auto", "learned"):
         return text
     g, w, c, r = (int(x) for x in text.split(","))
     return (g, w, c, r)
 
 
-def choose_schedule(args, eng, kt, sample):
+def train_selector(kt):
+    """The learned selector, trained by the library's CUDA kernels on the GB300 timing data."""
+    sys.path.insert(0, os.path.join(ROOT, "ktruss-explorer_gb300"))
+    import selector
+
+    t0 = time.perf_counter()
+    sel, losses = selector.train(selector.load(os.path.join(selector.DATA, "selector_train.npz")))
+    return sel, {"training_s": time.perf_counter() - t0, "training_graphs": 2000,
+                 "loss_first_last": [float(losses[0]), float(losses[-1])]}
+
+
+def choose_schedule(args, eng, kt, sample, target):
     """Sets the engine's schedule (and the host-buffer engine's) from --schedule; 'auto' runs the
-    autotuner on `sample()` = (n, src, dst) device tensors.  Returns the config record."""
+    autotuner on `sample()` = (n, src, dst) device tensors of other graphs of the same
+    distribution; 'learned' trains the selector and applies it to the features of `target()`, the
+    measured graph.  Returns the config record."""
     import torch
 
     choice = parse_schedule(args.schedule)
     rec = {"mode": args.schedule if isinstance(choice, str) else "fixed"}
+    if choice == "learned":
+        sel, info = train_selector(kt)
+        rec.update(info)
+        n, d_src, d_dst = target()
+        torch.cuda.synchronize()
+        feats = eng.features(d_src.data_ptr(), d_dst.data_ptr(), d_src.numel(), n)
+        choice = sel.predict(feats)[0].as_tuple()
+        sel.close()
     if choice == "auto":
         n, d_src, d_dst = sample()
         torch.cuda.synchronize()
@@ -290,7 +315,7 @@ def run_batch(args, world, rank, local):
         ns, us, vs, _ = kt.gen_batch(TUNE_SAMPLE["num_graphs"], b["n_min"], b["n_max"], TUNE_SAMPLE["seed"])
         return ns, dev(np.concatenate([us, vs])), dev(np.concatenate([vs, us]))
 
-    sched = choose_schedule(args, eng, kt, tune_sample)
+    sched = choose_schedule(args, eng, kt, tune_sample, lambda: (n, d_src, d_dst))
     torch.cuda.synchronize()
 
     def step():
@@ -324,6 +349,7 @@ def run_batch(args, world, rank, local):
     e2e_s = max_over_ranks((time.perf_counter() - t1) / args.steps, td, "cuda")
     if not np.array_equal(k2, kmax.view(np.uint32)):
         raise RuntimeError("host-buffer and device-buffer batches differ")
+    single = single_graph_path(kt, torch, eng, n, u, v, off, kmax.view(np.uint32), args.single_graphs)
     line = {"metric": "batched k-truss decomposition graphs/s", "value": G * world / (ms * 1e-3),
             "unit": "graphs/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
@@ -333,6 +359,7 @@ def run_batch(args, world, rank, local):
                        "k_max_max": int(kmax.max()), "peel_rounds": st.num_rounds, "peel_levels": st.num_levels,
                        "phase_ms": {"build": st.build_ms, "support": st.support_ms, "peel": st.peel_ms},
                        "generation_s": gen_s, "parallelism": f"replicas{world}", "schedule": sched,
+                       "single_graph_path": single,
                        "l2": "input entries 2x4x2m bytes > L2 (129 MB)"},
             "e2e": {"value": G * world / e2e_s, "unit": "graphs/s", "h2d_bytes_per_step": 8 * N + 4 * (G + 1),
                     "d2h_bytes_per_step": 4 * N + 4 * G},
@@ -342,6 +369,108 @@ def run_batch(args, world, rank, local):
     eng.close()
     if dist:
         td.destroy_process_group()
+
+
+def single_graph_path(kt, torch, eng, n, u, v, off, kmax, count):
+    """The plain path on the same graphs: the first `count` graphs of the batch decomposed one call
+    each (device buffers, default schedule, calls back to back), as graphs/s."""
+    G = min(count, len(off) - 1)
+    if G <= 0:
+        return None
+    lo = np.searchsorted(u, off[:G], side="left")
+    hi = np.searchsorted(u, off[1:G + 1], side="left")
+    parts_s, parts_d, spans = [], [], []
+    pos = 0
+    for g in range(G):
+        ug, vg = u[lo[g]:hi[g]] - off[g], v[lo[g]:hi[g]] - off[g]
+        parts_s += [ug, vg]
+        parts_d += [vg, ug]
+        spans.append((pos, 2 * len(ug), int(off[g + 1] - off[g])))
+        pos += 2 * len(ug)
+    dev = lambda a: torch.from_numpy(np.concatenate(a).astype(np.uint32).view(np.int32)).cuda()
+    d_s, d_d = dev(parts_s), dev(parts_d)
+    d_out = torch.empty(max(pos, 1), dtype=torch.int32, device="cuda")
+    d_k = torch.zeros(G, dtype=torch.int32, device="cuda")
+    saved = eng.schedule().as_tuple()
+    eng.set_schedule(*kt.schedule_default().as_tuple())
+    torch.cuda.synchronize()
+
+    def one_pass():
+        for g, (p0, N, ng) in enumerate(spans):
+            eng.decompose(d_s.data_ptr() + 4 * p0, d_d.data_ptr() + 4 * p0, N, ng, d_out.data_ptr() + 4 * p0,
+                          d_k.data_ptr() + 4 * g, sync=False)
+        torch.cuda.synchronize()
+
+    one_pass()
+    t0 = time.perf_counter()
+    one_pass()
+    secs = time.perf_counter() - t0
+    if not np.array_equal(d_k.cpu().numpy().view(np.uint32), kmax[:G]):
+        raise RuntimeError("single-graph calls and the batch disagree on k_max")
+    eng.set_schedule(*saved)
+    return {"graphs": G, "graphs_per_s": G / secs, "seconds": secs, "calls": G,
+            "note": "one kt_engine_decompose call per graph, default schedule, wall time of back-to-back calls"}
+
+
+def run_selector(args, world, rank, local):
+    """Learned selector on the 200 held-out graphs, live on this GPU: per graph, the support+peel
+    device time with the network's schedule against exhaustive autotuning of the same graph
+    (best of the 36 schedules) and the default schedule."""
+    import torch
+
+    import ktruss_gb300 as kt
+
+    if rank != 0:
+        return
+    torch.cuda.set_device(local)
+    sys.path.insert(0, os.path.join(ROOT, "ktruss-explorer_gb300"))
+    import selector
+
+    held = selector.load(os.path.join(selector.DATA, "selector_heldout.npz"))
+    sel, info = train_selector(kt)
+    eng = kt.Engine(local)
+    eng.set_selector(sel)
+    graphs = []
+    for spec in held["specs"]:
+        n, u, v = selector.make_graph(json.loads(str(spec)))
+        dev = lambda a: torch.from_numpy(np.ascontiguousarray(a, np.uint32).view(np.int32)).cuda()
+        graphs.append((n, len(u), dev(np.concatenate([u, v])), dev(np.concatenate([v, u]))))
+    torch.cuda.synchronize()
+    grid = kt.schedule_grid()
+    d_idx = kt.schedule_index(kt.schedule_default())
+    tuned = np.zeros(len(graphs))
+    default = np.zeros(len(graphs))
+    for i, (n, m, s_, d_) in enumerate(graphs):
+        eng.set_selector(None)
+        _, table = eng.autotune(s_.data_ptr(), d_.data_ptr(), s_.numel(), n, candidates=grid, repeats=args.steps)
+        ms = np.array([t for _, t in table])
+        tuned[i], default[i] = ms.min(), ms[d_idx]
+    eng.set_selector(sel)
+    out = torch.empty(max(s_.numel() for _, _, s_, _ in graphs), dtype=torch.int32, device="cuda")
+    kk = torch.zeros(1, dtype=torch.int32, device="cuda")
+    learned = np.full(len(graphs), np.inf)
+    for _ in range(args.warmup):
+        for n, m, s_, d_ in graphs:
+            eng.decompose(s_.data_ptr(), d_.data_ptr(), s_.numel(), n, out.data_ptr(), kk.data_ptr())
+    for _ in range(args.steps):
+        for i, (n, m, s_, d_) in enumerate(graphs):
+            eng.decompose(s_.data_ptr(), d_.data_ptr(), s_.numel(), n, out.data_ptr(), kk.data_ptr())
+            st = eng.stats()
+            learned[i] = min(learned[i], st.select_ms + st.support_ms + st.peel_ms)
+    ratio = learned.sum() / tuned.sum()
+    line = {"metric": "learned-selector time / exhaustively tuned time", "value": ratio, "unit": "ratio",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": learned.sum(),
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32 network, u32 peel",
+            "data": "synthetic",
+            "config": {"workload": "200 held-out graphs (Erdos-Renyi, R-MAT 12-18, Barabasi-Albert, random "
+                                   "geometric, planted cliques), support count + peel device time, best of "
+                                   f"{args.steps} runs per graph (the learned time includes the selector's "
+                                   "features, inference and read-back); selector trained on 2000 other graphs' "
+                                   "GB300 timings", "learned_ms": learned.sum(), "tuned_ms": tuned.sum(),
+                       "default_ms": default.sum(), "default_over_tuned": default.sum() / tuned.sum(),
+                       "gain_vs_default": default.sum() / learned.sum(), "tuning_runs": 36 * args.steps, **info}}
+    print(json.dumps(line), flush=True)
+    eng.close()
 
 
 def run_ours(args, world, rank, local):
@@ -371,7 +500,7 @@ def run_ours(args, world, rank, local):
         dev = lambda a: torch.from_numpy(np.ascontiguousarray(a, np.uint32).view(np.int32)).cuda()
         return ns, dev(np.concatenate([us, vs])), dev(np.concatenate([vs, us]))
 
-    sched = choose_schedule(args, eng, kt, tune_sample)
+    sched = choose_schedule(args, eng, kt, tune_sample, lambda: (n, d_src, d_dst))
     torch.cuda.synchronize()  # the engine stream does not order after torch's copies
 
     def step():
@@ -490,12 +619,15 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="rmat20", choices=sorted(WORKLOADS) + sorted(BATCHES))
+    ap.add_argument("--workload", default="rmat20", choices=sorted(WORKLOADS) + sorted(BATCHES) + ["selector"])
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--single-graphs", type=int, default=4096,
+                    help="batch workloads: graphs of the batch also decomposed one call each")
     ap.add_argument("--schedule", default=None,
                     help="kernel schedule: default, auto (autotune on a separate sample of the same "
-                         "distribution) or G,W,C,R; default: auto for batches, default for single graphs")
+                         "distribution), learned (the selector trained on the GB300 timing data) or G,W,C,R; "
+                         "default: auto for batches, default for single graphs")
     args = ap.parse_args()
     if args.schedule is None:
         args.schedule = "auto" if args.workload in BATCHES else "default"
@@ -503,6 +635,8 @@ def main():
     world, rank, local = dist_env()
     if args.impl == "reference":
         run_reference(args, world, rank)
+    elif args.workload == "selector":
+        run_selector(args, world, rank, local)
     elif args.workload in BATCHES:
         run_batch(args, world, rank, local)
     else:

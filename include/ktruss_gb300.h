@@ -174,6 +174,8 @@ typedef struct kt_stats {
                                     collection, row compaction, mark, process), barrier to
                                     barrier, as seen by its first block                        */
     float peel_kernel_ms;        /* CUDA-event time of the peel kernel launch alone            */
+    float select_ms;             /* learned selector: features, inference and the read-back of
+                                    its choice (0 without a selector); part of last_ms         */
 } kt_stats;
 
 /* Schedule of the engine's kernels (no counterpart in the reference, whose tuning knobs are the

@@ -159,15 +159,17 @@ int record_stop(kt_engine* e) {
     int rc = check_cuda(cudaEventRecord(e->ev_stop, e->stream), "record stop");
     if (rc) return rc;
     if ((rc = check_cuda(cudaEventSynchronize(e->ev_stop), "synchronize stop"))) return rc;
-    float a = 0, b = 0, c = 0;
-    if ((rc = check_cuda(cudaEventElapsedTime(&a, e->ev_start, e->ev_built), "elapsed time")) ||
+    float a = 0, b = 0, c = 0, d = 0;
+    if ((rc = check_cuda(cudaEventElapsedTime(&a, e->ev_start, e->ev_select), "elapsed time")) ||
+        (rc = check_cuda(cudaEventElapsedTime(&d, e->ev_select, e->ev_built), "elapsed time")) ||
         (rc = check_cuda(cudaEventElapsedTime(&b, e->ev_built, e->ev_counted), "elapsed time")) ||
         (rc = check_cuda(cudaEventElapsedTime(&c, e->ev_counted, e->ev_stop), "elapsed time")))
         return rc;
     e->stats.build_ms = a;
+    e->stats.select_ms = d;
     e->stats.support_ms = b;
     e->stats.peel_ms = c;
-    e->stats.last_ms = a + b + c;
+    e->stats.last_ms = a + b + c + d;
     return KT_OK;
 }
 
@@ -184,6 +186,7 @@ int run_decompose(kt_engine* e, const uint32_t* d_src, const uint32_t* d_dst, ui
     int rc;
     if ((rc = record_start(e))) return rc;
     if ((rc = kt::build_graph(e, d_src, d_dst, entries, n))) return rc;
+    if ((rc = record(e, e->ev_select))) return rc;
     if ((rc = kt::select_schedule(e))) return rc;
     if ((rc = record(e, e->ev_built))) return rc;
     if ((rc = kt::count_support(e))) return rc;
@@ -199,6 +202,7 @@ int run_ktruss(kt_engine* e, const uint32_t* d_src, const uint32_t* d_dst, uint6
     int rc;
     if ((rc = record_start(e))) return rc;
     if ((rc = kt::build_graph(e, d_src, d_dst, entries, n))) return rc;
+    if ((rc = record(e, e->ev_select))) return rc;
     if ((rc = record(e, e->ev_built))) return rc;
     if (k >= 3) {
         if ((rc = kt::count_support(e))) return rc;
@@ -236,6 +240,7 @@ int kt_engine_create(int device, kt_engine** out) {
         (rc = check_cuda(cudaEventCreate(&e->ev_stop), "create event")) ||
         (rc = check_cuda(cudaEventCreate(&e->ev_built), "create event")) ||
         (rc = check_cuda(cudaEventCreate(&e->ev_counted), "create event")) ||
+        (rc = check_cuda(cudaEventCreate(&e->ev_select), "create event")) ||
         (rc = check_cuda(cudaEventCreate(&e->ev_peel0), "create event")) ||
         (rc = check_cuda(cudaEventCreate(&e->ev_peel1), "create event")) ||
         (rc = check_cuda(cudaMalloc(&e->ctrl, sizeof(uint32_t) * kt::kCtrlWords), "allocate control block")) ||
@@ -259,6 +264,7 @@ int kt_engine_destroy(kt_engine* e) {
     if (e->ev_stop) cudaEventDestroy(e->ev_stop);
     if (e->ev_built) cudaEventDestroy(e->ev_built);
     if (e->ev_counted) cudaEventDestroy(e->ev_counted);
+    if (e->ev_select) cudaEventDestroy(e->ev_select);
     if (e->ev_peel0) cudaEventDestroy(e->ev_peel0);
     if (e->ev_peel1) cudaEventDestroy(e->ev_peel1);
     if (e->stream) cudaStreamDestroy(e->stream);
