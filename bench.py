@@ -578,6 +578,7 @@ def run_ours(args, world, rank, local):
                        "phase_ms": {"build": statistics.mean(build_ms), "support": sup_ms,
                                     "peel": statistics.mean(peel_ms)},
                        "peel_phase_ms": st.as_dict()["peel_phase_ms"], "compactions": st.compactions,
+                       "walk_entries": st.walk_entries,
                        "schedule": sched},
             "e2e": {"value": replica_throughput(m, world, e2e_s * 1e3), "unit": "edges/s", "h2d_bytes_per_step": 8 * N,
                     "d2h_bytes_per_step": 4 * N},

@@ -176,6 +176,9 @@ typedef struct kt_stats {
     float peel_kernel_ms;        /* CUDA-event time of the peel kernel launch alone            */
     float select_ms;             /* learned selector: features, inference and the read-back of
                                     its choice (0 without a selector); part of last_ms         */
+    uint64_t walk_entries;       /* adjacency entries in the rows of all queued edges: the
+                                    decrement work (a round that recounts instead does not walk
+                                    its queued rows)                                          */
 } kt_stats;
 
 /* Schedule of the engine's kernels (no counterpart in the reference, whose tuning knobs are the

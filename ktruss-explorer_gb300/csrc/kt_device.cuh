@@ -56,6 +56,7 @@ enum : uint32_t {
     kPEdges = 60,      // [4] edges queued for the round (chunked or long-row)
     kPChunks = 64,     // [4] u64 (words 64..71): work chunks claimed for the round; 64 bits
                        //     because a frontier of most edges can need more than 2^32 chunks
+    kPWalk = 72,       // u64 (words 72..73): row entries queued for walks over the whole peel
     kCtrlWords = 80,
 };
 

@@ -98,8 +98,8 @@ constexpr uint32_t kNullChunk = 0xffffffffu;
 
 // Queues edge e for round rr if `take`: stamps it, and splits the walk of its shorter row into
 // chunks of up to W = 1 << cw_shift entries (8, 16 or 32), each walked by W lanes, described by
-// {edge, other endpoint y, row position, entry count | kFirstChunk on the edge's first chunk}.  Rows are only compacted at level
-// starts, so the row measured here is the row walked.  Called by all 32 lanes of a warp
+// {edge, other endpoint y, row position, entry count | kFirstChunk on the edge's first chunk}.
+// Rows are only compacted at level starts, so the row measured here is the row walked.  Called by all 32 lanes of a warp
 // together: chunk slots are claimed with one atomic per warp.  If the chunk buffer is full, the
 // claimed slots are nulled and the edges go to the block-walked queue instead.
 __device__ __forceinline__ void push_edges(const PeelParams& P, uint32_t e, bool take, uint32_t rr) {
@@ -124,10 +124,12 @@ __device__ __forceinline__ void push_edges(const PeelParams& P, uint32_t e, bool
         if (lane >= (uint32_t)o) incl += t;
     }
     const uint32_t total = __shfl_sync(kFullMask, incl, 31);
+    const uint32_t walk = __reduce_add_sync(kFullMask, len);
     unsigned long long cb = 0;
     if (lane == 0) {
         cb = atomicAdd(reinterpret_cast<unsigned long long*>(P.ctrl + kPChunks) + slot, (unsigned long long)total);
         atomicAdd(P.ctrl + kPEdges + slot, __popc(mt));
+        atomicAdd(reinterpret_cast<unsigned long long*>(P.ctrl + kPWalk), (unsigned long long)walk);
     }
     cb = __shfl_sync(kFullMask, cb, 0);
     uint4* ch = P.ch[rr & 1];
@@ -188,7 +190,9 @@ __device__ __forceinline__ void peel_entries(const PeelParams& P, uint32_t e, ui
     for (int j = 0; j < NB; ++j) {
         if (act[j]) {
             ra[j] = P.rnd[a[j]];
-            if (ra[j] != 0 && ra[j] < r) act[j] = false;  // (x,w) removed earlier: triangle gone
+            // (x,w) removed earlier: the triangle is gone; (x,w) removed in this round with a
+            // smaller id: that edge (or a smaller one) owns the triangle.  Either way no search.
+            if ((ra[j] != 0 && ra[j] < r) || (ra[j] == r && a[j] < e)) act[j] = false;
         }
         if (!act[j]) n[j] = 0;
     }
@@ -827,6 +831,7 @@ int finish_stats(kt_engine* e) {
     if (e->stats_ready) return KT_OK;
     if (e->m == 0 || e->peel_mode == 2) {
         e->stats.compactions = 0;
+        e->stats.walk_entries = 0;
         e->stats.peel_kernel_ms = 0;
         for (int i = 0; i < 6; ++i) e->stats.peel_phase_ms[i] = 0;
         e->stats.k_max = 0;
@@ -849,6 +854,7 @@ int finish_stats(kt_engine* e) {
     e->stats.num_rounds = m ? e->h_ctrl[kPRounds] : 0;
     e->stats.num_levels = m ? e->h_ctrl[kPLevels] : 0;
     e->stats.compactions = e->h_ctrl[kPCompactions];
+    e->stats.walk_entries = (uint64_t)e->h_ctrl[kPWalk + 1] << 32 | e->h_ctrl[kPWalk];
     e->stats.peel_kernel_ms = 0;
     if (e->peel_timed &&
         (rc = check_cuda(cudaEventElapsedTime(&e->stats.peel_kernel_ms, e->ev_peel0, e->ev_peel1), "elapsed time")))

@@ -68,7 +68,8 @@ class Stats(ctypes.Structure):
                 ("kernel_launches", ctypes.c_uint64), ("last_ms", ctypes.c_float),
                 ("build_ms", ctypes.c_float), ("support_ms", ctypes.c_float), ("peel_ms", ctypes.c_float),
                 ("compactions", ctypes.c_uint32), ("peel_phase_ms", ctypes.c_float * 6),
-                ("peel_kernel_ms", ctypes.c_float), ("select_ms", ctypes.c_float)]
+                ("peel_kernel_ms", ctypes.c_float), ("select_ms", ctypes.c_float),
+                ("walk_entries", ctypes.c_uint64)]
 
     PHASES = ("init", "level_scan", "collect", "compaction", "mark", "process")
 
