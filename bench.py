@@ -473,6 +473,76 @@ def run_selector(args, world, rank, local):
     eng.close()
 
 
+def run_ingest(args, world, rank, local):
+    """Device-side TSV ingest: the R-MAT 20 graph as a 'dst src x' text file, parsed on the GPU
+    (text already in HBM: value; from the file through pinned staging: e2e) against the host
+    reader (cpu_baseline)."""
+    import tempfile
+
+    import torch
+
+    import ktruss_gb300 as kt
+
+    if rank != 0:
+        return
+    torch.cuda.set_device(local)
+    n, m, src, dst = make_graph("rmat20")
+    N = len(src)
+    with tempfile.TemporaryDirectory() as tmp:
+        path = os.path.join(tmp, "rmat20.tsv")
+        kt.write_coo_graph_to_file(kt.COOGraph(n, src, dst), path)
+        size = os.path.getsize(path)
+        t0 = time.perf_counter()
+        h = kt.create_coo_from_file(path)
+        host_s = time.perf_counter() - t0
+        eng = kt.Engine(local)
+        with open(path, "rb") as f:
+            text = torch.frombuffer(bytearray(f.read()), dtype=torch.uint8).cuda()
+        d_src = torch.empty(N, dtype=torch.int32, device="cuda")
+        d_dst = torch.empty(N, dtype=torch.int32, device="cuda")
+        torch.cuda.synchronize()
+        stream = torch.cuda.ExternalStream(eng.stream)
+        for _ in range(args.warmup):
+            eng.parse_tsv(text.data_ptr(), size, d_src.data_ptr(), d_dst.data_ptr(), N)
+        launches0 = eng.stats().kernel_launches
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with ClockSampler(local) as clk:
+            ev0.record(stream)
+            for _ in range(args.steps):
+                ne, nv = eng.parse_tsv(text.data_ptr(), size, d_src.data_ptr(), d_dst.data_ptr(), N)
+            ev1.record(stream)
+            torch.cuda.synchronize()
+        ms = ev0.elapsed_time(ev1) / args.steps
+        launches = eng.stats().kernel_launches - launches0
+        if ne != N or nv != h.num_nodes or not np.array_equal(d_src.cpu().numpy().view(np.uint32), h.src_idx):
+            raise RuntimeError("device and host readers differ")
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            eng.read_tsv(path, d_src.data_ptr(), d_dst.data_ptr(), N)
+        e2e_s = (time.perf_counter() - t0) / args.steps
+        eng.close()
+    hbm, hbm_kind = peaks()
+    alg = 2 * size + 8 * N  # text read by both passes, entries written once
+    gbs = alg / (ms * 1e-3) / 1e9
+    line = {"metric": "TSV ingest GB/s of text", "value": size / (ms * 1e-3) / 1e9, "unit": "GB/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u8 text, u32 entries", "data": "synthetic",
+            "config": {"workload": f"R-MAT 20 as a 'dst src x' TSV file ({size} bytes, {N} entries), parsed into "
+                                   "device entries", "bytes": size, "entries": N,
+                       "l2": "text larger than L2 (129 MB)"},
+            "e2e": {"value": size / e2e_s / 1e9, "unit": "GB/s", "h2d_bytes_per_step": size, "d2h_bytes_per_step": 0,
+                    "note": "file (page cache) -> pinned staging -> device -> parse, wall time"},
+            "gpu_launches": launches,
+            "roofline": {"bound": "hbm", "kernel": "k_tsv_count + k_tsv_parse + k_tsv_finish", "achieved": gbs,
+                         "peak": hbm, "peak_kind": hbm_kind, "unit": "GB/s", "frac": gbs / hbm, "traffic": None,
+                         "algorithmic_bytes": alg},
+            "cpu_baseline": {"value": size / host_s / 1e9, "unit": "GB/s", "cores": 1, "kind": "port",
+                             "sample": "the whole file through kt_read_tsv (the host restatement of "
+                                       "createCOOFromFile), once"},
+            "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+
+
 def run_ours(args, world, rank, local):
     import torch
 
@@ -620,7 +690,8 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="rmat20", choices=sorted(WORKLOADS) + sorted(BATCHES) + ["selector"])
+    ap.add_argument("--workload", default="rmat20",
+                    choices=sorted(WORKLOADS) + sorted(BATCHES) + ["selector", "ingest"])
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--single-graphs", type=int, default=4096,
@@ -638,6 +709,8 @@ def main():
         run_reference(args, world, rank)
     elif args.workload == "selector":
         run_selector(args, world, rank, local)
+    elif args.workload == "ingest":
+        run_ingest(args, world, rank, local)
     elif args.workload in BATCHES:
         run_batch(args, world, rank, local)
     else:

@@ -267,6 +267,19 @@ uint32_t kt_schedule_grid(kt_schedule* out, uint32_t cap);
 int kt_engine_autotune(kt_engine* engine, const uint32_t* d_src, const uint32_t* d_dst, uint64_t num_entries,
                        uint32_t num_nodes, const kt_schedule* candidates, uint32_t num_candidates,
                        uint32_t repeats, float* ms, kt_schedule* best);
+/* ---- device-side TSV ingest (replaces createCOOFromFile, graph.cu:37-79) ------------------
+ * The same format as kt_read_tsv - "dst src x" triples of unsigned decimal numbers separated by
+ * any whitespace, 1-based ids, x ignored - parsed on the device into 0-based entries in the
+ * caller's device buffers (entry i: d_src[i] = src-1, d_dst[i] = dst-1, in file order).
+ * *num_nodes = the largest id.  Statuses as kt_read_tsv (KT_ERR_IO for a malformed text, a 0
+ * id or an incomplete triple, KT_ERR_SELF_LOOP), and KT_ERR_CAPACITY when the text holds more
+ * than `capacity` entries (nothing is written then). */
+int kt_engine_parse_tsv(kt_engine* engine, const char* d_text, uint64_t bytes, uint32_t* d_src, uint32_t* d_dst,
+                        uint64_t capacity, uint64_t* num_entries, uint32_t* num_nodes);
+/* The same for a file: its bytes are copied to the device (pinned staging) and parsed there. */
+int kt_engine_read_tsv(kt_engine* engine, const char* path, uint32_t* d_src, uint32_t* d_dst, uint64_t capacity,
+                       uint64_t* num_entries, uint32_t* num_nodes);
+
 /* ---- learned schedule selector (no counterpart in the reference) ------------------------
  * A small MLP (16 -> 64 -> 64 -> 19, ReLU, FP32, hand-written CUDA kernels for inference,
  * training and Adam) that reads 16 statistics of a built graph and predicts its schedule from

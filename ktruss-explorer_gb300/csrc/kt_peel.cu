@@ -99,21 +99,25 @@ constexpr uint32_t kNullChunk = 0xffffffffu;
 // Queues edge e for round rr if `take`: stamps it, and splits the walk of its shorter row into
 // chunks of up to W = 1 << cw_shift entries (8, 16 or 32), each walked by W lanes, described by
 // {edge, other endpoint y, row position, entry count | kFirstChunk on the edge's first chunk}.
-// Rows are only compacted at level starts, so the row measured here is the row walked.  Called by all 32 lanes of a warp
+// Rows are only compacted at level starts, so the row measured here is the row walked.  An edge
+// queued with support 0 (`walk` false) has no triangle left whose other edges are alive or in
+// its round, so nothing to decrement: it gets one empty chunk, which only marks it removed.  Called by all 32 lanes of a warp
 // together: chunk slots are claimed with one atomic per warp.  If the chunk buffer is full, the
 // claimed slots are nulled and the edges go to the block-walked queue instead.
-__device__ __forceinline__ void push_edges(const PeelParams& P, uint32_t e, bool take, uint32_t rr) {
+__device__ __forceinline__ void push_edges(const PeelParams& P, uint32_t e, bool take, uint32_t rr, bool walk) {
     const uint32_t mt = __ballot_sync(kFullMask, take);
     if (!mt) return;
     uint32_t nch = 0, y = 0, base = 0, len = 0;
     if (take) {
         P.rnd[e] = rr;
-        const uint32_t u = P.e_src[e], v = P.o_col[e];
-        const uint32_t lu = P.s_len[u], lv = P.s_len[v];
-        const bool ux = lu <= lv;
-        y = ux ? v : u;
-        base = P.s_ptr[ux ? u : v];
-        len = ux ? lu : lv;
+        if (walk) {
+            const uint32_t u = P.e_src[e], v = P.o_col[e];
+            const uint32_t lu = P.s_len[u], lv = P.s_len[v];
+            const bool ux = lu <= lv;
+            y = ux ? v : u;
+            base = P.s_ptr[ux ? u : v];
+            len = ux ? lu : lv;
+        }
         nch = len ? (len + (1u << P.cw_shift) - 1) >> P.cw_shift : 1;
     }
     const uint32_t lane = lane_id(), slot = rr & 3;
@@ -124,12 +128,12 @@ __device__ __forceinline__ void push_edges(const PeelParams& P, uint32_t e, bool
         if (lane >= (uint32_t)o) incl += t;
     }
     const uint32_t total = __shfl_sync(kFullMask, incl, 31);
-    const uint32_t walk = __reduce_add_sync(kFullMask, len);
+    const uint32_t walked = __reduce_add_sync(kFullMask, len);
     unsigned long long cb = 0;
     if (lane == 0) {
         cb = atomicAdd(reinterpret_cast<unsigned long long*>(P.ctrl + kPChunks) + slot, (unsigned long long)total);
         atomicAdd(P.ctrl + kPEdges + slot, __popc(mt));
-        atomicAdd(reinterpret_cast<unsigned long long*>(P.ctrl + kPWalk), (unsigned long long)walk);
+        atomicAdd(reinterpret_cast<unsigned long long*>(P.ctrl + kPWalk), (unsigned long long)walked);
     }
     cb = __shfl_sync(kFullMask, cb, 0);
     uint4* ch = P.ch[rr & 1];
@@ -228,8 +232,9 @@ __device__ __forceinline__ void peel_entries(const PeelParams& P, uint32_t e, ui
                 if (rb != r) qb = atomicSub(&P.sup[b], 1u) == km2;
             }
         }
-        push_edges(P, a[j], qa, r + 1);
-        push_edges(P, b, qb, r + 1);
+        // a decrement queues an edge with support k-3, which is 0 only at level 3
+        push_edges(P, a[j], qa, r + 1, km2 != 1);
+        push_edges(P, b, qb, r + 1, km2 != 1);
     }
 }
 
@@ -359,7 +364,8 @@ __device__ __forceinline__ void collect(const PeelParams& P, uint32_t thr, uint3
                                         uint64_t nthreads) {
     for (uint64_t j0 = start + tid - lane_id(); j0 < P.m; j0 += nthreads) {
         const uint64_t j = j0 + lane_id();
-        push_edges(P, (uint32_t)j, j < P.m && P.sup[j] <= thr, rr);
+        const uint32_t sj = j < P.m ? P.sup[j] : kDead;
+        push_edges(P, (uint32_t)j, sj <= thr, rr, sj != 0);
     }
 }
 
@@ -463,7 +469,7 @@ __global__ void __launch_bounds__(kPeelThreads, 1) k_peel(PeelParams P) {
                             mn = sj < mn ? sj : mn;
                             min_id = (uint32_t)j < min_id ? (uint32_t)j : min_id;
                         }
-                        push_edges(P, (uint32_t)j, sj != kDead && sj <= kg - 3, rr);
+                        push_edges(P, (uint32_t)j, sj != kDead && sj <= kg - 3, rr, sj != 0);
                     }
                 }
             }

@@ -156,6 +156,9 @@ def lib() -> ctypes.CDLL:
         L.kt_selector_predict.argtypes = [_VP, _FP, ctypes.c_uint32, ctypes.POINTER(Schedule)]
         L.kt_engine_features.argtypes = [_VP, _VP, _VP, ctypes.c_uint64, ctypes.c_uint32, _FP]
         L.kt_engine_set_selector.argtypes = [_VP, _VP]
+        _U64P = ctypes.POINTER(ctypes.c_uint64)
+        L.kt_engine_parse_tsv.argtypes = [_VP, _VP, ctypes.c_uint64, _VP, _VP, ctypes.c_uint64, _U64P, _U32P]
+        L.kt_engine_read_tsv.argtypes = [_VP, ctypes.c_char_p, _VP, _VP, ctypes.c_uint64, _U64P, _U32P]
         L.kt_set_schedule.argtypes = [ctypes.POINTER(Schedule)]
         L.kt_get_schedule.argtypes = [ctypes.POINTER(Schedule)]
         L.kt_schedule_grid.argtypes = [ctypes.POINTER(Schedule), ctypes.c_uint32]
@@ -406,6 +409,20 @@ class Engine:
         out = np.zeros(SELECTOR_FEATURES, np.float32)
         _check(lib().kt_engine_features(self._h, d_src, d_dst, num_entries, num_nodes, _fp(out)))
         return out
+
+    def parse_tsv(self, d_text: int, num_bytes: int, d_src: int, d_dst: int, capacity: int) -> tuple:
+        """Parses TSV text already on the device into device entries; returns (entries, num_nodes)."""
+        ne, nn = ctypes.c_uint64(0), ctypes.c_uint32(0)
+        _check(lib().kt_engine_parse_tsv(self._h, d_text, num_bytes, d_src, d_dst, capacity, ctypes.byref(ne),
+                                         ctypes.byref(nn)))
+        return ne.value, nn.value
+
+    def read_tsv(self, path: str, d_src: int, d_dst: int, capacity: int) -> tuple:
+        """Reads a TSV file into device entries (parsed on the device); returns (entries, num_nodes)."""
+        ne, nn = ctypes.c_uint64(0), ctypes.c_uint32(0)
+        _check(lib().kt_engine_read_tsv(self._h, os.fsencode(path), d_src, d_dst, capacity, ctypes.byref(ne),
+                                        ctypes.byref(nn)))
+        return ne.value, nn.value
 
     def set_selector(self, selector: Optional["Selector"]) -> None:
         """Attach a learned selector (its schedule is used by every decomposition) or detach (None)."""
