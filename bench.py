@@ -227,12 +227,12 @@ def run_reference(args, world, rank):
 
 
 def parse_schedule(text):
-    """'default', 'auto' or 'G,W,C,R' (support group, chunk width, compaction percent, recount
-    percent)."""
+    """'default', 'auto', 'learned' or 'G,W,C,R[,B]' (support group, chunk width, compaction
+    percent, recount percent, peel blocks per SM; B defaults to 0 = by L2 fit)."""
     if text in ("default", "auto", "learned"):
         return text
-    g, w, c, r = (int(x) for x in text.split(","))
-    return (g, w, c, r)
+    vals = [int(x) for x in text.split(",")]
+    return tuple(vals + [0] * (5 - len(vals)))
 
 
 def train_selector(kt):
@@ -277,7 +277,8 @@ def choose_schedule(args, eng, kt, sample, target):
         choice = kt.schedule_default().as_tuple()
     eng.set_schedule(*choice)
     kt.set_schedule(*choice)
-    rec["support_group"], rec["chunk_width"], rec["compact_percent"], rec["recount_percent"] = choice
+    (rec["support_group"], rec["chunk_width"], rec["compact_percent"], rec["recount_percent"],
+     rec["peel_blocks"]) = choice
     return rec
 
 

@@ -194,9 +194,12 @@ typedef struct kt_schedule {
                                   the surviving edges from scratch (the reference's full
                                   recount) instead of decrementing it per destroyed triangle
                                   (its affected-edge recount, made exact): 1..100, or 0 = never */
+    uint32_t peel_blocks;      /* peel kernel blocks per SM: 1 (64 registers a thread), 2 (32
+                                  registers, twice the warps: hides DRAM latency once the graph
+                                  outgrows L2), or 0 = 2 when the oriented CSR exceeds L2, else 1 */
 } kt_schedule;
 
-/* The default schedule {8, 32, 85, 50}. */
+/* The default schedule {8, 32, 85, 50, 0}. */
 kt_schedule kt_schedule_default(void);
 
 /* Creates an engine on `device` with its own non-blocking CUDA stream. */
@@ -254,8 +257,8 @@ int kt_engine_get_schedule(kt_engine* engine, kt_schedule* schedule);
 int kt_set_schedule(const kt_schedule* schedule);
 int kt_get_schedule(kt_schedule* schedule);
 /* The autotuner's built-in grid of schedules: support_group {4, 8, 16} x chunk_width
- * {8, 16, 32} x compact_percent {0, 85} x recount_percent {0, 50} (36).  Writes min(36, cap)
- * schedules to `out` (may be NULL) and returns 36. */
+ * {8, 16, 32} x compact_percent {0, 85} x recount_percent {0, 50}, peel_blocks 0 (36).  Writes
+ * min(36, cap) schedules to `out` (may be NULL) and returns 36. */
 uint32_t kt_schedule_grid(kt_schedule* out, uint32_t cap);
 /* Autotuner (no counterpart in the reference).  Decomposes the given device graph — or a batch
  * given as the union of its graphs — once per candidate schedule and `repeats` times each

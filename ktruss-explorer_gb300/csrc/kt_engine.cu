@@ -310,7 +310,7 @@ int kt_engine_ktruss(kt_engine* e, const uint32_t* d_src, const uint32_t* d_dst,
     return KT_OK;
 }
 
-kt_schedule kt_schedule_default(void) { return kt_schedule{8, 32, 85, 50}; }
+kt_schedule kt_schedule_default(void) { return kt_schedule{8, 32, 85, 50, 0}; }
 
 int kt_engine_set_schedule(kt_engine* e, const kt_schedule* s) {
     kt::clear_error();
@@ -323,6 +323,7 @@ int kt_engine_set_schedule(kt_engine* e, const kt_schedule* s) {
         return fail(KT_ERR_INVALID_ARG, "compact_percent must be 0..99 (got %u)", s->compact_percent);
     if (s->recount_percent > 100)
         return fail(KT_ERR_INVALID_ARG, "recount_percent must be 0..100 (got %u)", s->recount_percent);
+    if (s->peel_blocks > 2) return fail(KT_ERR_INVALID_ARG, "peel_blocks must be 0, 1 or 2 (got %u)", s->peel_blocks);
     e->sched = *s;
     return KT_OK;
 }
@@ -357,7 +358,7 @@ uint32_t kt_schedule_grid(kt_schedule* out, uint32_t cap) {
         for (uint32_t w : widths)
             for (uint32_t c : compact)
                 for (uint32_t rc : recount) {
-                    if (out && i < cap) out[i] = kt_schedule{g, w, c, rc};
+                    if (out && i < cap) out[i] = kt_schedule{g, w, c, rc, 0};
                     ++i;
                 }
     return i;

@@ -85,14 +85,15 @@ class Schedule(ctypes.Structure):
     the alive edges from which a round recounts the survivors instead of decrementing (0 = never).
     Results never depend on it."""
     _fields_ = [("support_group", ctypes.c_uint32), ("chunk_width", ctypes.c_uint32),
-                ("compact_percent", ctypes.c_uint32), ("recount_percent", ctypes.c_uint32)]
+                ("compact_percent", ctypes.c_uint32), ("recount_percent", ctypes.c_uint32),
+                ("peel_blocks", ctypes.c_uint32)]
 
     def as_tuple(self) -> tuple:
-        return (self.support_group, self.chunk_width, self.compact_percent, self.recount_percent)
+        return (self.support_group, self.chunk_width, self.compact_percent, self.recount_percent, self.peel_blocks)
 
     def __repr__(self) -> str:
-        return ("Schedule(support_group=%d, chunk_width=%d, compact_percent=%d, recount_percent=%d)"
-                % self.as_tuple())
+        return ("Schedule(support_group=%d, chunk_width=%d, compact_percent=%d, recount_percent=%d, "
+                "peel_blocks=%d)" % self.as_tuple())
 
 
 _LIB = None
@@ -382,8 +383,8 @@ class Engine:
                                       int(sync)))
 
     def set_schedule(self, support_group: int = 8, chunk_width: int = 32, compact_percent: int = 85,
-                     recount_percent: int = 50) -> None:
-        s = Schedule(support_group, chunk_width, compact_percent, recount_percent)
+                     recount_percent: int = 50, peel_blocks: int = 0) -> None:
+        s = Schedule(support_group, chunk_width, compact_percent, recount_percent, peel_blocks)
         _check(lib().kt_engine_set_schedule(self._h, ctypes.byref(s)))
 
     def schedule(self) -> Schedule:
@@ -531,9 +532,9 @@ def schedule_default() -> Schedule:
 
 
 def set_schedule(support_group: int = 8, chunk_width: int = 32, compact_percent: int = 85,
-                 recount_percent: int = 50) -> None:
+                 recount_percent: int = 50, peel_blocks: int = 0) -> None:
     """Schedule of the engine behind the host-buffer calls (ktruss, decompose, decompose_batch)."""
-    s = Schedule(support_group, chunk_width, compact_percent, recount_percent)
+    s = Schedule(support_group, chunk_width, compact_percent, recount_percent, peel_blocks)
     _check(lib().kt_set_schedule(ctypes.byref(s)))
 
 

@@ -17,7 +17,8 @@ GRAPHS = [
     ("ws8000", lambda: kt.gen_ws(8000, 10, 0.1, 14)),
 ]
 
-SCHEDULES = list(itertools.product((4, 8, 16, 32), (8, 16, 32), (0, 50, 85), (0, 1, 50)))
+SCHEDULES = list(itertools.product((4, 8, 16, 32), (8, 16, 32), (0, 50, 85), (0, 1, 50), (0,))) + \
+    list(itertools.product((8,), (8, 32), (0, 85), (0, 50), (1, 2)))
 
 
 @pytest.fixture(scope="module")
@@ -35,25 +36,26 @@ def test_every_schedule_matches_oracle(name, make, torch):
     d_dst = torch.from_numpy(dst.view(np.int32)).cuda()
     d_out = torch.empty(len(src), dtype=torch.int32, device="cuda")
     d_k = torch.zeros(1, dtype=torch.int32, device="cuda")
-    for g, w, c, rc in SCHEDULES:
-        eng.set_schedule(g, w, c, rc)
-        assert eng.schedule().as_tuple() == (g, w, c, rc)
+    for sched in SCHEDULES:
+        g, w, c, rc, pb = sched
+        eng.set_schedule(*sched)
+        assert eng.schedule().as_tuple() == sched
         d_out.fill_(-1)
         torch.cuda.synchronize()  # the engine runs on its own stream
         eng.decompose(d_src.data_ptr(), d_dst.data_ptr(), len(src), n, d_out.data_ptr(), d_k.data_ptr())
-        assert int(d_k.item()) == ref["k_max"], (g, w, c, rc)
-        assert np.array_equal(d_out.cpu().numpy().view(np.uint32), ref["truss"]), (g, w, c, rc)
+        assert int(d_k.item()) == ref["k_max"], sched
+        assert np.array_equal(d_out.cpu().numpy().view(np.uint32), ref["truss"]), sched
         st = eng.stats()
         assert st.compactions == 0 or c != 0
 
 
-@pytest.mark.parametrize("w,rc", [(8, 0), (16, 0), (32, 50), (8, 1)])
-def test_single_k_with_narrow_chunks(w, rc, torch):
+@pytest.mark.parametrize("w,rc,pb", [(8, 0, 0), (16, 0, 2), (32, 50, 2), (8, 1, 1)])
+def test_single_k_with_narrow_chunks(w, rc, pb, torch):
     n, u, v = kt.plant_cliques(*kt.gen_ba(5000, 8, 21), 2, 20, 40, 22)
     src, dst = both_directions(u, v)
     ref = oracle.decompose(n, src, dst, method="peel")
     eng = kt.Engine(0)
-    eng.set_schedule(16, w, 85, rc)
+    eng.set_schedule(16, w, 85, rc, pb)
     d_src = torch.from_numpy(src.view(np.int32)).cuda()
     d_dst = torch.from_numpy(dst.view(np.int32)).cuda()
     keep = torch.empty(len(src), dtype=torch.uint8, device="cuda")
@@ -67,7 +69,7 @@ def test_batch_with_narrow_chunks(torch):
     n, u, v, off = kt.gen_batch(24, 500, 4000, 31)
     src, dst = both_directions(u, v)
     eng = kt.Engine(0)
-    eng.set_schedule(4, 8, 50, 25)
+    eng.set_schedule(4, 8, 50, 25, 2)
     d_src = torch.from_numpy(src.view(np.int32)).cuda()
     d_dst = torch.from_numpy(dst.view(np.int32)).cuda()
     d_off = torch.from_numpy(off.view(np.int32)).cuda()
@@ -80,8 +82,8 @@ def test_batch_with_narrow_chunks(torch):
     assert np.array_equal(d_out.cpu().numpy().view(np.uint32), ref["truss"])
 
 
-@pytest.mark.parametrize("bad", [(2, 32, 85, 0), (64, 32, 85, 0), (8, 4, 85, 0), (8, 64, 85, 0), (8, 32, 100, 0),
-                                 (8, 32, 85, 101)])
+@pytest.mark.parametrize("bad", [(2, 32, 85, 0, 0), (64, 32, 85, 0, 0), (8, 4, 85, 0, 0), (8, 64, 85, 0, 0),
+                                 (8, 32, 100, 0, 0), (8, 32, 85, 101, 0), (8, 32, 85, 50, 3)])
 def test_invalid_schedule_rejected(bad):
     eng = kt.Engine(0)
     before = eng.schedule().as_tuple()
@@ -102,8 +104,8 @@ def _clique_union(sizes):
 
 
 @pytest.mark.parametrize("sizes", [[20] * 300, [100, 100, 64]], ids=["many_small", "few_large"])
-@pytest.mark.parametrize("w,rc", [(8, 0), (32, 0), (8, 50)])
-def test_chunk_buffer_overflow(sizes, w, rc, torch):
+@pytest.mark.parametrize("w,rc,pb", [(8, 0, 0), (32, 0, 2), (8, 50, 2)])
+def test_chunk_buffer_overflow(sizes, w, rc, pb, torch):
     """A level whose whole frontier is every edge of many cliques needs more chunks than the
     buffer holds (m + 4096 on an engine sized for this graph): the rest is walked by warps (many
     edges) or blocks (few edges).  Every edge of a c-clique has truss number c."""
@@ -116,7 +118,7 @@ def test_chunk_buffer_overflow(sizes, w, rc, torch):
     expect = np.concatenate([np.full(s * (s - 1) // 2, s, np.uint32) for s in sizes])
     eng = kt.Engine(0)
     eng.reserve(n, len(src))
-    eng.set_schedule(8, w, 85, rc)
+    eng.set_schedule(8, w, 85, rc, pb)
     d_src = torch.from_numpy(src.view(np.int32)).cuda()
     d_dst = torch.from_numpy(dst.view(np.int32)).cuda()
     d_out = torch.empty(len(src), dtype=torch.int32, device="cuda")

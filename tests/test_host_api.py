@@ -165,7 +165,7 @@ def test_cli_missing_graph_fails(tmp_path):
 
 
 def test_default_schedule():
-    assert kt.schedule_default().as_tuple() == (8, 32, 85, 50)
+    assert kt.schedule_default().as_tuple() == (8, 32, 85, 50, 0)
 
 
 def test_schedule_grid():

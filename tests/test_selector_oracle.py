@@ -50,5 +50,5 @@ def test_grid_order_is_variant_then_recount():
     assert len(grid) == so.SCHEDULES
     for v in range(so.V):
         a, b = grid[2 * v], grid[2 * v + 1]
-        assert a[:3] == b[:3] and a[3] == 0 and b[3] == 50
+        assert a[:3] == b[:3] and a[3] == 0 and b[3] == 50 and a[4] == b[4] == 0
     assert kt.schedule_index(kt.schedule_default()) == 2 * 11 + 1  # variant (8, 32, 85), recount on
