@@ -116,7 +116,9 @@ __global__ void __launch_bounds__(kSortThreads) k_radix_hist(const uint64_t* __r
 }
 
 // Stable scatter of one 2048-key tile: each warp ranks its 256 consecutive keys in eight
-// 32-key steps with __match_any_sync; warps are then offset by the counts of earlier warps.
+// 32-key steps with __match_any_sync; warps are then offset by the counts of earlier warps.  The
+// tile is first arranged in digit order in shared memory, then written out so that consecutive
+// threads store consecutive positions of each digit's run (coalesced stores).
 __global__ void __launch_bounds__(kSortThreads) k_radix_scatter(const uint64_t* __restrict__ kin,
                                                                   const uint32_t* __restrict__ vin,
                                                                   uint64_t* __restrict__ kout,
@@ -125,12 +127,17 @@ __global__ void __launch_bounds__(kSortThreads) k_radix_scatter(const uint64_t* 
                                                                   const uint32_t* __restrict__ hist,
                                                                   uint32_t num_blocks) {
     __shared__ uint32_t wh[kSortWarps][256];
-    __shared__ uint32_t goff[256];
+    __shared__ uint32_t goff[256];   // global start of each digit's run for this tile
+    __shared__ uint32_t toff[256];   // start of each digit's run inside the tile
+    __shared__ uint32_t ws[33];
+    __shared__ uint64_t skey[kSortTile];
+    __shared__ uint32_t sval[kSortTile];
     const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
     for (uint32_t i = threadIdx.x; i < kSortWarps * 256; i += kSortThreads) (&wh[0][0])[i] = 0;
     goff[threadIdx.x] = hist[(uint64_t)threadIdx.x * num_blocks + blockIdx.x];
     __syncthreads();
-    const uint64_t wbase = (uint64_t)blockIdx.x * kSortTile + (uint64_t)warp * kSortWarpKeys;
+    const uint64_t tbase = (uint64_t)blockIdx.x * kSortTile;
+    const uint64_t wbase = tbase + (uint64_t)warp * kSortWarpKeys;
     uint64_t key[kSortSteps];
     uint32_t val[kSortSteps], dig[kSortSteps], rk[kSortSteps];
 #pragma unroll
@@ -149,6 +156,7 @@ __global__ void __launch_bounds__(kSortThreads) k_radix_scatter(const uint64_t* 
         rk[s] = base + __popc(peers & lanemask_lt());
     }
     __syncthreads();
+    uint32_t count = 0;  // keys of digit threadIdx.x in the tile
     {
         uint32_t run = 0;
 #pragma unroll
@@ -157,16 +165,49 @@ __global__ void __launch_bounds__(kSortThreads) k_radix_scatter(const uint64_t* 
             wh[w][threadIdx.x] = run;
             run += c;
         }
+        count = run;
+    }
+    // exclusive scan of the tile's digit counts (one digit per thread)
+    {
+        uint32_t x = count;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(kFullMask, x, o);
+            if (lane >= (uint32_t)o) x += y;
+        }
+        if (lane == 31) ws[warp] = x;
+        __syncthreads();
+        if (warp == 0) {
+            const uint32_t w = lane < kSortWarps ? ws[lane] : 0u;
+            uint32_t t = w;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(kFullMask, t, o);
+                if (lane >= (uint32_t)o) t += y;
+            }
+            if (lane < kSortWarps) ws[lane] = t - w;
+        }
+        __syncthreads();
+        toff[threadIdx.x] = ws[warp] + x - count;
     }
     __syncthreads();
 #pragma unroll
     for (int s = 0; s < kSortSteps; ++s) {
-        uint32_t d = dig[s];
+        const uint32_t d = dig[s];
         if (d < 256) {
-            uint32_t pos = goff[d] + wh[warp][d] + rk[s];
-            kout[pos] = key[s];
-            if (vin) vout[pos] = val[s];
+            const uint32_t lp = toff[d] + wh[warp][d] + rk[s];
+            skey[lp] = key[s];
+            sval[lp] = val[s];
         }
+    }
+    __syncthreads();
+    const uint32_t valid = (uint32_t)min((uint64_t)kSortTile, n - tbase);
+    for (uint32_t i = threadIdx.x; i < valid; i += kSortThreads) {
+        const uint64_t k = skey[i];
+        const uint32_t d = (uint32_t)(k >> shift) & 255u;
+        const uint32_t pos = goff[d] + (i - toff[d]);
+        kout[pos] = k;
+        if (vin) vout[pos] = sval[i];
     }
 }
 
