@@ -196,7 +196,8 @@ typedef struct kt_schedule {
                                   (its affected-edge recount, made exact): 1..100, or 0 = never */
     uint32_t peel_blocks;      /* peel kernel blocks per SM: 1 (64 registers a thread), 2 (32
                                   registers, twice the warps: hides DRAM latency once the graph
-                                  outgrows L2), or 0 = 2 when the oriented CSR exceeds L2, else 1 */
+                                  outgrows L2), or 0 = 2 when the oriented CSR of a single graph
+                                  exceeds L2, else 1 (batches: 1)                                 */
 } kt_schedule;
 
 /* The default schedule {8, 32, 85, 50, 0}. */

@@ -503,7 +503,10 @@ int kt_engine_decompose_batch(kt_engine* e, const uint32_t* d_src, const uint32_
     int rc = check_cuda(cudaSetDevice(e->device), "cudaSetDevice");
     if (rc) return rc;
     // the union of disjoint graphs: its truss numbers are each graph's own
-    if ((rc = run_decompose(e, d_src, d_dst, num_entries, num_nodes, d_truss_per_entry, nullptr))) return rc;
+    e->batch_call = true;
+    rc = run_decompose(e, d_src, d_dst, num_entries, num_nodes, d_truss_per_entry, nullptr);
+    e->batch_call = false;
+    if (rc) return rc;
     if ((rc = kt::emit_graph_kmax(e, d_src, d_dst, d_vertex_offsets, num_graphs, d_truss_per_entry,
                                   d_k_max_per_graph)))
         return rc;
@@ -551,7 +554,10 @@ int kt_decompose_batch(const uint32_t* src, const uint32_t* dst, uint64_t num_en
     if (N && ((rc = check_cuda(cudaMemcpyAsync(e->in_src, src, N * 4, cudaMemcpyHostToDevice, e->stream), "H2D")) ||
               (rc = check_cuda(cudaMemcpyAsync(e->in_dst, dst, N * 4, cudaMemcpyHostToDevice, e->stream), "H2D"))))
         return rc;
-    if ((rc = run_decompose(e, e->in_src, e->in_dst, N, num_nodes, e->out_u32, nullptr))) return rc;
+    e->batch_call = true;
+    rc = run_decompose(e, e->in_src, e->in_dst, N, num_nodes, e->out_u32, nullptr);
+    e->batch_call = false;
+    if (rc) return rc;
     if ((rc = kt::emit_graph_kmax(e, e->in_src, e->in_dst, d_off, num_graphs, e->out_u32, d_kmax))) return rc;
     if (N && (rc = check_cuda(cudaMemcpyAsync(truss_per_entry, e->out_u32, N * 4, cudaMemcpyDeviceToHost, e->stream),
                               "D2H")))

@@ -86,6 +86,7 @@ struct kt_engine {
     uint32_t vb = 1;  // bits per rank in sort keys
 
     kt_schedule sched{8, 32, 85, 50, 0};  // kernel schedule (kt_engine_set_schedule)
+    bool batch_call = false;           // the current call decomposes a batch of separate graphs
     kt_selector* selector = nullptr;   // learned schedule selector (kt_engine_set_selector)
     uint32_t* sel_stats = nullptr;     // 16 u64 graph statistics for the selector's features
     float* sel_feat = nullptr;         // the 16 features

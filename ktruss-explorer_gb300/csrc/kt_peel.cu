@@ -706,8 +706,11 @@ int launch_peel(kt_engine* e, uint32_t single_k) {
     if ((rc = check_launch(e, "k_init_peel_ctrl"))) return rc;
     int l2 = 0;
     if ((rc = check_cuda(cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, e->device), "L2 size"))) return rc;
+    // automatic choice: two blocks per SM when the oriented CSR outgrows L2 - but not for a batch,
+    // whose many small graphs keep their walks local (batch4096: peel 303 ms with one block per
+    // SM, 342 ms with two)
     const bool wide = e->sched.peel_blocks == 2 ||
-                      (e->sched.peel_blocks == 0 && 4 * ((uint64_t)e->m + e->n + 1) > (uint64_t)l2);  // CSR beyond L2
+                      (e->sched.peel_blocks == 0 && !e->batch_call && 4 * ((uint64_t)e->m + e->n + 1) > (uint64_t)l2);
     const void* kernel = wide ? (const void*)k_peel<2> : (const void*)k_peel<1>;
     int per_sm = 0;
     if ((rc = check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kPeelThreads, 0),
