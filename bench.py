@@ -355,6 +355,7 @@ def run_batch(args, world, rank, local):
     for _ in range(args.steps):
         _, k2 = kt.decompose_batch(h_src, h_dst, n, off, out=h_out)
     e2e_s = max_over_ranks((time.perf_counter() - t1) / args.steps, td, "cuda")
+    ls = kt.last_stats()
     if not np.array_equal(k2, kmax.view(np.uint32)):
         raise RuntimeError("host-buffer and device-buffer batches differ")
     single = single_graph_path(kt, torch, eng, n, u, v, off, kmax.view(np.uint32), args.single_graphs)
@@ -371,7 +372,9 @@ def run_batch(args, world, rank, local):
                        "single_graph_path": single,
                        "l2": "input entries 2x4x2m bytes > L2 (129 MB)"},
             "e2e": {"value": G * world / e2e_s, "unit": "graphs/s", "h2d_bytes_per_step": 8 * N + 4 * (G + 1),
-                    "d2h_bytes_per_step": 4 * N + 4 * G},
+                    "d2h_bytes_per_step": 4 * N + 4 * G, "ms_per_step": e2e_s * 1e3,
+                    "last_call_device_ms": {"copy_in": ls.copy_in_ms, "decompose": ls.last_ms,
+                                            "copy_out_and_kmax": ls.copy_out_ms}},
             "gpu_launches": launches, "clocks": clk.summary()}
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -626,6 +629,7 @@ def run_ours(args, world, rank, local):
     for _ in range(args.steps):
         _, k2 = kt.decompose(g, out=out_np)
     e2e_s = (time.perf_counter() - t0) / args.steps
+    ls = kt.last_stats()
     if dist:
         e2e_s = max_over_ranks(e2e_s, td, "cuda")
     assert k2 == k_max
@@ -660,7 +664,9 @@ def run_ours(args, world, rank, local):
                        "walk_entries": st.walk_entries,
                        "schedule": sched},
             "e2e": {"value": replica_throughput(m, world, e2e_s * 1e3), "unit": "edges/s", "h2d_bytes_per_step": 8 * N,
-                    "d2h_bytes_per_step": 4 * N},
+                    "d2h_bytes_per_step": 4 * N, "ms_per_step": e2e_s * 1e3,
+                    "last_call_device_ms": {"copy_in": ls.copy_in_ms, "decompose": ls.last_ms,
+                                            "copy_out": ls.copy_out_ms}},
             "gpu_launches": launches // args.steps * args.steps,
             "roofline": {"bound": "hbm", "kernel": "k_peel", "achieved": pk_gbs, "peak": hbm,
                          "peak_kind": hbm_kind, "unit": "GB/s", "frac": pk_gbs / hbm,

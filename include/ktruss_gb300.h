@@ -179,6 +179,10 @@ typedef struct kt_stats {
     uint64_t walk_entries;       /* adjacency entries in the rows of all queued edges: the
                                     decrement work (a round that recounts instead does not walk
                                     its queued rows)                                          */
+    float copy_in_ms;            /* host-buffer calls (kt_decompose, kt_decompose_batch): device
+                                    time of the input copies host -> device                   */
+    float copy_out_ms;           /*   and of the output copies device -> host (plus the emit
+                                    of per-graph k_max in a batch)                            */
 } kt_stats;
 
 /* Schedule of the engine's kernels (no counterpart in the reference, whose tuning knobs are the
@@ -253,6 +257,9 @@ int kt_engine_level_log(kt_engine* engine, uint32_t* k, uint32_t* alive, uint32_
  * ranges above); kt_engine_get_schedule reads it. */
 int kt_engine_set_schedule(kt_engine* engine, const kt_schedule* schedule);
 int kt_engine_get_schedule(kt_engine* engine, kt_schedule* schedule);
+/* Statistics of the last call of the host-buffer entry points (kt_ktruss, kt_decompose,
+ * kt_decompose_batch), including the device time of their copies (copy_in_ms, copy_out_ms). */
+int kt_last_stats(kt_stats* stats);
 /* Schedule of the engine behind the host-buffer entry points (kt_ktruss, kt_decompose,
  * kt_decompose_batch). */
 int kt_set_schedule(const kt_schedule* schedule);

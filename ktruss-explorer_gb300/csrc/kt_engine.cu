@@ -173,6 +173,14 @@ int record_stop(kt_engine* e) {
     return KT_OK;
 }
 
+// Device time of the input and output copies of a host-buffer call (events ev_copy[0..3]; the
+// stream must have drained).
+int copy_times(kt_engine* e) {
+    int rc = check_cuda(cudaEventElapsedTime(&e->stats.copy_in_ms, e->ev_copy[0], e->ev_copy[1]), "elapsed time");
+    if (!rc) rc = check_cuda(cudaEventElapsedTime(&e->stats.copy_out_ms, e->ev_copy[2], e->ev_copy[3]), "elapsed time");
+    return rc;
+}
+
 int fill_graph_stats(kt_engine* e) {
     e->stats.num_nodes = e->n;
     e->stats.num_edges = e->m;
@@ -241,6 +249,10 @@ int kt_engine_create(int device, kt_engine** out) {
         (rc = check_cuda(cudaEventCreate(&e->ev_built), "create event")) ||
         (rc = check_cuda(cudaEventCreate(&e->ev_counted), "create event")) ||
         (rc = check_cuda(cudaEventCreate(&e->ev_select), "create event")) ||
+        (rc = check_cuda(cudaEventCreate(&e->ev_copy[0]), "create event")) ||
+        (rc = check_cuda(cudaEventCreate(&e->ev_copy[1]), "create event")) ||
+        (rc = check_cuda(cudaEventCreate(&e->ev_copy[2]), "create event")) ||
+        (rc = check_cuda(cudaEventCreate(&e->ev_copy[3]), "create event")) ||
         (rc = check_cuda(cudaEventCreate(&e->ev_peel0), "create event")) ||
         (rc = check_cuda(cudaEventCreate(&e->ev_peel1), "create event")) ||
         (rc = check_cuda(cudaMalloc(&e->ctrl, sizeof(uint32_t) * kt::kCtrlWords), "allocate control block")) ||
@@ -265,6 +277,8 @@ int kt_engine_destroy(kt_engine* e) {
     if (e->ev_built) cudaEventDestroy(e->ev_built);
     if (e->ev_counted) cudaEventDestroy(e->ev_counted);
     if (e->ev_select) cudaEventDestroy(e->ev_select);
+    for (cudaEvent_t ev : e->ev_copy)
+        if (ev) cudaEventDestroy(ev);
     if (e->ev_peel0) cudaEventDestroy(e->ev_peel0);
     if (e->ev_peel1) cudaEventDestroy(e->ev_peel1);
     if (e->stream) cudaStreamDestroy(e->stream);
@@ -333,6 +347,16 @@ int kt_engine_get_schedule(kt_engine* e, kt_schedule* s) {
     if (!e || !s) return fail(KT_ERR_INVALID_ARG, "kt_engine_get_schedule: null argument");
     *s = e->sched;
     return KT_OK;
+}
+
+int kt_last_stats(kt_stats* stats) {
+    kt::clear_error();
+    if (!stats) return fail(KT_ERR_INVALID_ARG, "kt_last_stats: null argument");
+    kt_engine* e = nullptr;
+    int rc = default_engine(&e);
+    if (rc) return rc;
+    std::lock_guard<std::mutex> lock(g_default_mu);
+    return kt_engine_stats(e, stats);
 }
 
 int kt_set_schedule(const kt_schedule* s) {
@@ -548,26 +572,30 @@ int kt_decompose_batch(const uint32_t* src, const uint32_t* dst, uint64_t num_en
     uint32_t* d_off = e->aux;
     uint32_t* d_kmax = e->aux + num_graphs + 1;
     const uint64_t N = num_entries;
-    if ((rc = check_cuda(cudaMemcpyAsync(d_off, vertex_offsets, sizeof(uint32_t) * (num_graphs + 1),
+    if ((rc = record(e, e->ev_copy[0])) ||
+        (rc = check_cuda(cudaMemcpyAsync(d_off, vertex_offsets, sizeof(uint32_t) * (num_graphs + 1),
                                          cudaMemcpyHostToDevice, e->stream), "H2D")))
         return rc;
     if (N && ((rc = check_cuda(cudaMemcpyAsync(e->in_src, src, N * 4, cudaMemcpyHostToDevice, e->stream), "H2D")) ||
               (rc = check_cuda(cudaMemcpyAsync(e->in_dst, dst, N * 4, cudaMemcpyHostToDevice, e->stream), "H2D"))))
         return rc;
+    if ((rc = record(e, e->ev_copy[1]))) return rc;
     e->batch_call = true;
     rc = run_decompose(e, e->in_src, e->in_dst, N, num_nodes, e->out_u32, nullptr);
     e->batch_call = false;
     if (rc) return rc;
     if ((rc = kt::emit_graph_kmax(e, e->in_src, e->in_dst, d_off, num_graphs, e->out_u32, d_kmax))) return rc;
+    if ((rc = record(e, e->ev_copy[2]))) return rc;
     if (N && (rc = check_cuda(cudaMemcpyAsync(truss_per_entry, e->out_u32, N * 4, cudaMemcpyDeviceToHost, e->stream),
                               "D2H")))
         return rc;
     if ((rc = check_cuda(cudaMemcpyAsync(k_max_per_graph, d_kmax, sizeof(uint32_t) * num_graphs,
                                          cudaMemcpyDeviceToHost, e->stream), "D2H")) ||
-        (rc = check_cuda(cudaStreamSynchronize(e->stream), "synchronize")))
+        (rc = record(e, e->ev_copy[3])) || (rc = check_cuda(cudaStreamSynchronize(e->stream), "synchronize")))
         return rc;
     e->stats_ready = false;
-    return kt::finish_stats(e);
+    if ((rc = kt::finish_stats(e))) return rc;
+    return copy_times(e);
 }
 
 int kt_decompose(const kt_coo* graph, uint32_t* truss_per_entry, uint32_t* k_max, const kt_config* config) {
@@ -583,16 +611,20 @@ int kt_decompose(const kt_coo* graph, uint32_t* truss_per_entry, uint32_t* k_max
     if ((rc = check_cuda(cudaSetDevice(e->device), "cudaSetDevice"))) return rc;
     const uint64_t N = graph->num_edges;
     if ((rc = kt::reserve(e, std::max(graph->num_nodes, e->cap_nodes), std::max(N, e->cap_entries)))) return rc;
+    if ((rc = record(e, e->ev_copy[0]))) return rc;
     if (N) {
         if ((rc = check_cuda(cudaMemcpyAsync(e->in_src, graph->src_idx, N * 4, cudaMemcpyHostToDevice, e->stream), "H2D")) ||
             (rc = check_cuda(cudaMemcpyAsync(e->in_dst, graph->dst_idx, N * 4, cudaMemcpyHostToDevice, e->stream), "H2D")))
             return rc;
     }
+    if ((rc = record(e, e->ev_copy[1]))) return rc;
     if ((rc = run_decompose(e, e->in_src, e->in_dst, N, graph->num_nodes, e->out_u32, nullptr))) return rc;
+    if ((rc = record(e, e->ev_copy[2]))) return rc;
     if (N && (rc = check_cuda(cudaMemcpyAsync(truss_per_entry, e->out_u32, N * 4, cudaMemcpyDeviceToHost, e->stream), "D2H")))
         return rc;
+    if ((rc = record(e, e->ev_copy[3]))) return rc;
     if ((rc = check_cuda(cudaStreamSynchronize(e->stream), "synchronize"))) return rc;
-    if ((rc = kt::finish_stats(e))) return rc;
+    if ((rc = kt::finish_stats(e)) || (rc = copy_times(e))) return rc;
     if (k_max) *k_max = e->stats.k_max;
     return KT_OK;
 }

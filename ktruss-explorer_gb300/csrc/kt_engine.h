@@ -14,6 +14,7 @@ struct kt_engine {
     cudaStream_t stream = nullptr;
     cudaEvent_t ev_start = nullptr, ev_stop = nullptr, ev_built = nullptr, ev_counted = nullptr;
     cudaEvent_t ev_select = nullptr;  // after the build, before the selector's choice
+    cudaEvent_t ev_copy[4] = {};      // host-buffer calls: around the input and output copies
     cudaEvent_t ev_peel0 = nullptr, ev_peel1 = nullptr;  // around the peel kernel launch
     bool peel_timed = false;
     uint64_t launches = 0;

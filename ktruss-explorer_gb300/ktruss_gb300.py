@@ -69,7 +69,7 @@ class Stats(ctypes.Structure):
                 ("build_ms", ctypes.c_float), ("support_ms", ctypes.c_float), ("peel_ms", ctypes.c_float),
                 ("compactions", ctypes.c_uint32), ("peel_phase_ms", ctypes.c_float * 6),
                 ("peel_kernel_ms", ctypes.c_float), ("select_ms", ctypes.c_float),
-                ("walk_entries", ctypes.c_uint64)]
+                ("walk_entries", ctypes.c_uint64), ("copy_in_ms", ctypes.c_float), ("copy_out_ms", ctypes.c_float)]
 
     PHASES = ("init", "level_scan", "collect", "compaction", "mark", "process")
 
@@ -132,6 +132,7 @@ def lib() -> ctypes.CDLL:
         L.kt_engine_ktruss.argtypes = [_VP, _VP, _VP, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32, _VP,
                                        ctypes.c_int]
         L.kt_engine_stats.argtypes = [_VP, ctypes.POINTER(Stats)]
+        L.kt_last_stats.argtypes = [ctypes.POINTER(Stats)]
         L.kt_engine_selftest_barrier_timeout.argtypes = [_VP, ctypes.c_uint64]
         L.kt_engine_decompose_batch.argtypes = [_VP, _VP, _VP, ctypes.c_uint64, ctypes.c_uint32, _VP, ctypes.c_uint32,
                                                 _VP, _VP, ctypes.c_int]
@@ -550,6 +551,14 @@ def schedule_grid() -> list:
     arr = (Schedule * n)()
     lib().kt_schedule_grid(arr, n)
     return [arr[i] for i in range(n)]
+
+
+def last_stats() -> Stats:
+    """Statistics of the last host-buffer call (the engine behind kt_ktruss / kt_decompose /
+    kt_decompose_batch)."""
+    s = Stats()
+    _check(lib().kt_last_stats(ctypes.byref(s)))
+    return s
 
 
 def decompose_batch(src, dst, num_nodes: int, vertex_offsets, out: Optional[np.ndarray] = None):
