@@ -214,9 +214,10 @@ def run_reference(args, world, rank):
         t_full = vol["plain_alive_sum"] / rate
         value = m / t_full
         unit = "edges/s"
-        desc = (f"first {samples[0]['passes']} of {vol['plain_passes']} count-and-prune passes of the chained "
-                f"decomposition ({samples[0]['alive_sum']} of {vol['plain_alive_sum']} alive-edge visits), "
-                f"{samples[0]['seconds']:.1f} s per step; scaled by alive-edge volume")
+        desc = (f"the start of the reference's chained decomposition: {samples[0]['passes']} complete of "
+                f"{vol['plain_passes']} count-and-prune passes plus the edges a cut pass had counted "
+                f"({samples[0]['alive_sum']} of {vol['plain_alive_sum']} alive-edge visits, graph set-up "
+                f"included), {samples[0]['seconds']:.1f} s per step; scaled by alive-edge volume")
     else:
         value, unit, t_full = rate, "alive-edge-visits/s", None
         desc = "first passes of the chained decomposition (pass volume unknown: not scaled)"
