@@ -247,8 +247,9 @@ def train_selector(kt):
     import selector
 
     t0 = time.perf_counter()
-    sel, losses = selector.train(selector.load(os.path.join(selector.DATA, "selector_train.npz")))
-    return sel, {"training_s": time.perf_counter() - t0, "training_graphs": 2000,
+    data = selector.load_training()
+    sel, losses = selector.train(data)
+    return sel, {"training_s": time.perf_counter() - t0, "training_graphs": int(len(data["times"])),
                  "loss_first_last": [float(losses[0]), float(losses[-1])]}
 
 

@@ -2,6 +2,7 @@
 
     python ktruss-explorer_gb300/selector.py collect --count 2000 --seed 1 --out data/selector_train.npz
     python ktruss-explorer_gb300/selector.py collect --count 200 --seed 2 --out data/selector_heldout.npz
+    python ktruss-explorer_gb300/selector.py collect --families batch --count 300 --seed 3 --out data/selector_batch.npz
     python ktruss-explorer_gb300/selector.py evaluate
 
 `collect` generates seeded graphs - Erdos-Renyi, R-MAT scale 12-18, Barabasi-Albert, random
@@ -28,12 +29,18 @@ import ktruss_gb300 as kt  # noqa: E402
 
 DATA = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data")
 FAMILIES = ("er", "rmat", "ba", "rgg", "cliques")
+# Unions of 16-128 graphs of the batch distribution (kt_gen_batch), as kt_engine_decompose_batch
+# sees them: a separate training set, so that the network also knows batches.
+BATCH_FAMILIES = ("batch",)
 
 
-def graph_spec(index: int, seed: int) -> dict:
+def graph_spec(index: int, seed: int, families=FAMILIES) -> dict:
     """Deterministic recipe of training graph `index` of the set with this seed."""
     rng = np.random.default_rng([seed, index])
-    fam = FAMILIES[index % len(FAMILIES)]
+    fam = families[index % len(families)]
+    if fam == "batch":
+        return dict(family=fam, graphs=int(round(2 ** rng.uniform(4, 7))), n_min=500, n_max=50000,
+                    seed=int(rng.integers(1, 2**31)))
     gseed = int(rng.integers(1, 2**31))
     logn = lambda lo, hi: int(round(2 ** rng.uniform(lo, hi)))
     if fam == "er":
@@ -52,6 +59,9 @@ def graph_spec(index: int, seed: int) -> dict:
 def make_graph(spec: dict):
     """(num_nodes, u, v) of a spec, u < v."""
     f = spec["family"]
+    if f == "batch":
+        n, u, v, _ = kt.gen_batch(spec["graphs"], spec["n_min"], spec["n_max"], spec["seed"])
+        return n, u, v
     if f == "er":
         n = spec["n"]
         return kt.gen_er(n, spec["degree"] / (n - 1), spec["seed"])
@@ -70,7 +80,7 @@ def make_graph(spec: dict):
     return kt.plant_cliques(*g, spec["count"], spec["min_size"], min(spec["max_size"], n), spec["seed"] + 1)
 
 
-def collect(count: int, seed: int, device: int = 0, repeats: int = 1, log=None) -> dict:
+def collect(count: int, seed: int, device: int = 0, repeats: int = 1, log=None, families=FAMILIES) -> dict:
     """Features and the times of all grid schedules for `count` seeded graphs."""
     import torch
 
@@ -82,7 +92,7 @@ def collect(count: int, seed: int, device: int = 0, repeats: int = 1, log=None) 
     specs, edges = [], np.zeros(count, np.int64)
     t0 = time.time()
     for i in range(count):
-        spec = graph_spec(i, seed)
+        spec = graph_spec(i, seed, families)
         n, u, v = make_graph(spec)
         src = torch.from_numpy(np.concatenate([u, v]).view(np.int32)).cuda()
         dst = torch.from_numpy(np.concatenate([v, u]).view(np.int32)).cuda()
@@ -106,6 +116,16 @@ def save(path: str, data: dict) -> None:
 def load(path: str) -> dict:
     with np.load(path, allow_pickle=False) as z:
         return {k: z[k] for k in z.files}
+
+
+def load_training() -> dict:
+    """The training data in data/: the 2000 single graphs, plus the batch unions when present."""
+    d = load(os.path.join(DATA, "selector_train.npz"))
+    extra = os.path.join(DATA, "selector_batch.npz")
+    if os.path.exists(extra):
+        b = load(extra)
+        d = {k: np.concatenate([d[k], b[k]]) for k in ("features", "times", "specs", "edges")}
+    return d
 
 
 def train(data: dict, epochs: int = 300, batch: int = 64, lr: float = 3e-3, seed: int = 1, device: int = 0):
@@ -139,18 +159,21 @@ def main():
     c.add_argument("--seed", type=int, default=1)
     c.add_argument("--repeats", type=int, default=1)
     c.add_argument("--out", required=True)
+    c.add_argument("--families", default="graphs", choices=["graphs", "batch"],
+                   help="graphs: ER, R-MAT, BA, RGG, planted cliques; batch: unions of batch graphs")
     e = sub.add_parser("evaluate")
-    e.add_argument("--train", default=os.path.join(DATA, "selector_train.npz"))
+    e.add_argument("--train", default=None, help="training set (default: data/, with the batch unions)")
     e.add_argument("--heldout", default=os.path.join(DATA, "selector_heldout.npz"))
     e.add_argument("--epochs", type=int, default=300)
     args = ap.parse_args()
     if args.cmd == "collect":
-        d = collect(args.count, args.seed, repeats=args.repeats, log=lambda s: print(s, flush=True))
+        fams = BATCH_FAMILIES if args.families == "batch" else FAMILIES
+        d = collect(args.count, args.seed, repeats=args.repeats, log=lambda s: print(s, flush=True), families=fams)
         save(args.out, d)
         print(f"wrote {args.out}: {args.count} graphs", flush=True)
     else:
         t0 = time.time()
-        sel, losses = train(load(args.train), epochs=args.epochs)
+        sel, losses = train(load(args.train) if args.train else load_training(), epochs=args.epochs)
         r = evaluate(sel, load(args.heldout))
         r["train_s"] = time.time() - t0
         r["loss_first_last"] = [float(losses[0]), float(losses[-1])]

@@ -138,7 +138,7 @@ def test_trained_selector_gains_over_default_on_heldout_graphs():
     """Trained on the training graphs' timings, the network's choices on the held-out graphs take
     less total time than the default schedule; its regret against per-graph exhaustive tuning is
     reported in the assertion message."""
-    train = sel_mod.load(os.path.join(DATA, "selector_train.npz"))
+    train = sel_mod.load_training()
     held = sel_mod.load(os.path.join(DATA, "selector_heldout.npz"))
     s, losses = sel_mod.train(train, epochs=300)
     assert losses[-1] < 0.8 * losses[0]
