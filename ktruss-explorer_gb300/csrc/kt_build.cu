@@ -26,6 +26,7 @@ namespace {
 
 constexpr int kThreads = 256;
 constexpr uint32_t kBigRow = 2048;  // rows this long are compacted by a whole block
+constexpr uint32_t kTinyRow = 8;    // rows this short are compacted by one thread
 
 inline uint32_t grid_for(uint64_t n, int threads = kThreads) {
     uint64_t b = (n + threads - 1) / threads;
@@ -166,9 +167,9 @@ __global__ void k_entry_eid(const uint32_t* __restrict__ sorted_entry, const uin
 }
 
 // First rank whose symmetric row has at least `thr` entries (rows grow with rank: ranks are
-// ascending degree), written to ctrl[kCtrlBigRow].
+// ascending degree), written to ctrl[slot].
 __global__ void k_find_big_row(const uint32_t* __restrict__ s_ptr, uint32_t n, uint32_t thr,
-                               uint32_t* __restrict__ ctrl) {
+                               uint32_t* __restrict__ ctrl, uint32_t slot) {
     uint32_t lo = 0, len = n;
     while (len > 0) {
         uint32_t half = len >> 1;
@@ -180,7 +181,7 @@ __global__ void k_find_big_row(const uint32_t* __restrict__ s_ptr, uint32_t n, u
             len = half;
         }
     }
-    ctrl[kCtrlBigRow] = lo;
+    ctrl[slot] = lo;
 }
 
 unsigned bits_for(uint64_t n) {
@@ -298,11 +299,15 @@ int build_graph(kt_engine* e, const uint32_t* d_src, const uint32_t* d_dst, uint
         count_launch(e);
         if ((rc = check_launch(e, "k_entry_eid"))) return rc;
     }
-    k_find_big_row<<<1, 1, 0, st>>>(e->s_ptr, n, kBigRow, e->ctrl);
+    k_find_big_row<<<1, 1, 0, st>>>(e->s_ptr, n, kBigRow, e->ctrl, kCtrlBigRow);
+    count_launch(e);
+    if ((rc = check_launch(e, "k_find_big_row"))) return rc;
+    k_find_big_row<<<1, 1, 0, st>>>(e->s_ptr, n, kTinyRow + 1, e->ctrl, kCtrlTinyRow);
     count_launch(e);
     if ((rc = check_launch(e, "k_find_big_row"))) return rc;
     if ((rc = sync_and_check(e))) return rc;
     e->big_row = e->h_ctrl[kCtrlBigRow];
+    e->tiny_row = e->h_ctrl[kCtrlTinyRow];
     return KT_OK;
 }
 

@@ -39,6 +39,7 @@ enum : uint32_t {
     kCtrlItems0 = 12,     // work-item queue counters
     kCtrlItems1 = 13,
     kCtrlBigRow = 14,     // first rank whose symmetric row is long (block-wide compaction)
+    kCtrlTinyRow = 15,    // first rank whose symmetric row is not tiny (thread-wise compaction below)
     // Persistent peel kernel: barrier, outputs, and rings of per-round / per-level counters
     // (slot r % 4 belongs to round r; slot (r+2) % 4 is cleared during round r).
     kPBarCount = 16,

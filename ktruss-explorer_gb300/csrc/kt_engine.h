@@ -54,6 +54,7 @@ struct kt_engine {
     uint4* chunks1 = nullptr;
     uint32_t cap_chunks = 0;
     uint32_t big_row = 0;         // ranks >= big_row have rows of kBigRow entries or more
+    uint32_t tiny_row = 0;        // ranks < tiny_row have rows of at most 8 entries
     // Scratch for scans and sort histograms.
     uint32_t* scan_tmp = nullptr;
     size_t scan_tmp_words = 0;

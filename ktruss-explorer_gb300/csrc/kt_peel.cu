@@ -81,7 +81,7 @@ struct PeelParams {
     uint32_t* level_front;
     uint32_t cap_rounds;
     uint32_t cap_levels;
-    uint32_t n, m, big_row;
+    uint32_t n, m, big_row, tiny_row;
     uint32_t cw_shift;  // log2 of the chunk width (row entries per work chunk): 3, 4 or 5
     uint32_t compact_num;  // rows are compacted once alive edges < compact_num/100 of the count
                            // at the last compaction (0: never)
@@ -101,9 +101,10 @@ constexpr uint32_t kNullChunk = 0xffffffffu;
 // {edge, other endpoint y, row position, entry count | kFirstChunk on the edge's first chunk}.
 // Rows are only compacted at level starts, so the row measured here is the row walked.  An edge
 // queued with support 0 (`walk` false) has no triangle left whose other edges are alive or in
-// its round, so nothing to decrement: it gets one empty chunk, which only marks it removed.  Called by all 32 lanes of a warp
-// together: chunk slots are claimed with one atomic per warp.  If the chunk buffer is full, the
-// claimed slots are nulled and the edges go to the block-walked queue instead.
+// its round, so nothing to decrement: it gets one empty chunk, which only marks it removed.
+// Called by all 32 lanes of a warp together: chunk slots are claimed with one atomic per warp.
+// If the chunk buffer is full, the claimed slots are nulled and the edges go to the
+// block-walked queue instead.
 __device__ __forceinline__ void push_edges(const PeelParams& P, uint32_t e, bool take, uint32_t rr, bool walk) {
     const uint32_t mt = __ballot_sync(kFullMask, take);
     if (!mt) return;
@@ -291,15 +292,49 @@ __device__ __forceinline__ void slot_context(const PeelParams& P, uint32_t e, ui
     *len = ux ? lu : lv;
 }
 
-// In-place ordered compaction of the symmetric rows: warps take the short rows [0, big_row),
-// blocks the long rows [big_row, n).  Entries of edges removed in rounds <= r_done are dropped.
-// Each step reads before any write of the step, and writes never pass the read position.
+// In-place ordered compaction of the symmetric rows: threads take the tiny rows [0, tiny_row)
+// (at most 8 entries, read four at a time), warps the short rows [tiny_row, big_row), blocks the
+// long rows [big_row, n).  Entries of edges removed in rounds <= r_done are dropped.  Each step
+// reads before any write of the step, and writes never pass the read position.
 __device__ void compact_rows(const PeelParams& P, uint32_t r_done, uint32_t* warp_cnt) {
     const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
     const uint32_t gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
     const uint32_t big = P.big_row < P.n ? P.big_row : P.n;
-    for (uint32_t row = gwarp; row < big; row += nwarps) {
+    const uint32_t tiny = P.tiny_row < big ? P.tiny_row : big;
+    for (uint32_t row = blockIdx.x * blockDim.x + threadIdx.x; row < tiny; row += gridDim.x * blockDim.x) {
+        const uint32_t base = P.s_ptr[row], len = P.s_len[row];
+        uint32_t w = 0;
+        for (uint32_t i0 = 0; i0 < len; i0 += 4) {
+            uint32_t c[4], id[4];
+            bool keep[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                keep[q] = i0 + q < len;
+                if (keep[q]) {
+                    c[q] = P.s_col[base + i0 + q];
+                    id[q] = P.s_eid[base + i0 + q];
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                if (keep[q]) {
+                    const uint32_t rr = P.rnd[id[q]];
+                    keep[q] = rr == 0 || rr > r_done;
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                if (keep[q]) {
+                    P.s_col[base + w] = c[q];
+                    P.s_eid[base + w] = id[q];
+                    ++w;
+                }
+            }
+        }
+        P.s_len[row] = w;
+    }
+    for (uint32_t row = tiny + gwarp; row < big; row += nwarps) {
         const uint32_t base = P.s_ptr[row], len = P.s_len[row];
         uint32_t w = 0;
         for (uint32_t i0 = 0; i0 < len; i0 += 32) {
@@ -746,6 +781,7 @@ int launch_peel(kt_engine* e, uint32_t single_k) {
     P.n = e->n;
     P.m = e->m;
     P.big_row = e->big_row;
+    P.tiny_row = e->tiny_row < e->big_row ? e->tiny_row : e->big_row;
     P.cw_shift = e->sched.chunk_width == 8 ? 3u : e->sched.chunk_width == 16 ? 4u : 5u;
     P.compact_num = e->sched.compact_percent;
     P.recount_num = e->sched.recount_percent;
