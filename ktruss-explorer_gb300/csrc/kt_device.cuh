@@ -25,19 +25,9 @@ enum : uint32_t {
 // Layout of the device control block (uint32 words unless noted).
 enum : uint32_t {
     kCtrlError = 0,
-    kCtrlCount0 = 1,      // frontier / compaction counters
-    kCtrlCount1 = 2,
-    kCtrlMin = 3,         // minimum support over alive edges
-    kCtrlKmax = 4,
-    kCtrlRound = 5,
-    kCtrlLevel = 6,
-    kCtrlAlive = 7,
-    kCtrlBarrier = 8,     // grid barrier arrival counter
-    kCtrlBarrierGen = 9,  // grid barrier generation
+    // words 1-9, 12, 13 and 21-27 are unused
     kCtrlTriLo = 10,      // 64-bit triangle counter (lo, hi)
     kCtrlTriHi = 11,
-    kCtrlItems0 = 12,     // work-item queue counters
-    kCtrlItems1 = 13,
     kCtrlBigRow = 14,     // first rank whose symmetric row is long (block-wide compaction)
     kCtrlTinyRow = 15,    // first rank whose symmetric row is not tiny (thread-wise compaction below)
     // Persistent peel kernel: barrier, outputs, and rings of per-round / per-level counters

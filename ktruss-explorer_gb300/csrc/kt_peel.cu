@@ -19,13 +19,15 @@
 //
 // One round is one phase followed by one grid barrier.  When an edge is queued (its support
 // fell below the threshold, or it is in a level's first frontier) it is stamped with the next
-// round number and the walk of its shorter row is split into chunks of up to 32 entries; in
-// the round every warp takes chunks, so a long row is spread over many warps and no warp walks
-// more than its share.  Per neighbour w of the shorter row's vertex x, the edge (y,w) is found
-// by a binary search in an oriented row.  A removed edge's support is set to
-// kDead, so a level's scan of the alive list reads one array; that scan also collects the
-// frontier of level k_last+1, and only when that level turns out to be empty does a second
-// pass collect the frontier of the next non-empty level.
+// round number and the walk of its shorter row is split into chunks of up to W entries (the
+// schedule's chunk width, 8, 16 or 32); in the round every warp takes chunks, so a long row is
+// spread over many warps and no warp walks more than its share.  Per neighbour w of the shorter
+// row's vertex x, the edge (y,w) is found by a binary search in an oriented row.  A round whose
+// frontier holds at least the schedule's recount share of the alive edges instead removes the
+// frontier at once and recounts the survivors' support (the reference's full recount).  A removed
+// edge's support is set to kDead, so a level's scan of the alive list reads one array; that scan
+// also collects the frontier of level k_last+1, and only when that level turns out to be empty
+// does a second pass collect the frontier of the next non-empty level.
 // Symmetric rows are compacted in place at a level start once enough edges have been removed
 // since the last compaction, so the walks see few removed entries.
 //
@@ -45,11 +47,7 @@ constexpr int kThreads = 256;          // helper kernels
 #ifndef KT_PEEL_THREADS
 #define KT_PEEL_THREADS 1024
 #endif
-#ifndef KT_PEEL_BATCH
-#define KT_PEEL_BATCH 1
-#endif
 constexpr int kPeelThreads = KT_PEEL_THREADS;  // persistent kernel: one or two blocks per SM
-constexpr int kBatch = KT_PEEL_BATCH;  // row entries in flight per thread
 constexpr uint64_t kPeelTimeoutNs = 10ull * 1000 * 1000 * 1000;
 
 inline uint32_t grid_for(uint64_t n, int threads = kThreads) {
@@ -159,10 +157,11 @@ __device__ __forceinline__ void push_edges(const PeelParams& P, uint32_t e, bool
 
 // Entries of a removed edge e's shorter row (vertex x): called by all 32 lanes of a warp
 // together (each lane may serve a different edge); the lane at position `pos` of its group
-// handles row positions base + t0 + pos + j*step (j < NB) that are below base + len,
-// so that the memory chains of different entries overlap.  For a neighbour w of x, edge (x,w) is
-// s_eid at the entry and edge (y,w) is found by a binary search in an oriented row (w in N+(y)
-// if w > y, else y in N+(w)); the NB searches advance in lockstep.  Edge states during round r:
+// handles row positions base + t0 + pos + j*step (j < NB) that are below base + len, the NB
+// searches advancing in lockstep (the kernel uses NB = 1: wider batches measured slower, their
+// registers spill).  For a neighbour w of x, edge (x,w) is s_eid at the entry and edge (y,w) is
+// found by a binary search in an oriented row (w in N+(y) if w > y, else y in N+(w)).  Edge
+// states during round r:
 // rnd 0 = alive, r+1 = alive but queued for the next round, r = removed in this round,
 // 1..r-1 = removed earlier.  A triangle is skipped if one of its edges was removed earlier or if
 // a smaller-id edge of this round owns it; otherwise each surviving edge loses one support, and
