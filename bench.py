@@ -43,6 +43,8 @@ WORKLOADS = {
     # R-MAT scale 20, edge factor 16, (a,b,c,d) = (0.57,0.19,0.19,0.05), symmetrized, deduplicated,
     # self loops removed; seed 1
     "rmat20": dict(scale=20, ef=16, a=0.57, b=0.19, c=0.19, seed=1),
+    "rmat22": dict(scale=22, ef=16, a=0.57, b=0.19, c=0.19, seed=1),
+    "rmat21": dict(scale=21, ef=16, a=0.57, b=0.19, c=0.19, seed=1),
     "rmat18": dict(scale=18, ef=16, a=0.57, b=0.19, c=0.19, seed=1),
     "rmat16": dict(scale=16, ef=16, a=0.57, b=0.19, c=0.19, seed=1),
     # stress: R-MAT scale 24, edge factor 32, same (a,b,c,d), plus 16 planted cliques of 64-512
