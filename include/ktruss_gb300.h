@@ -278,6 +278,17 @@ uint32_t kt_schedule_grid(kt_schedule* out, uint32_t cap);
 int kt_engine_autotune(kt_engine* engine, const uint32_t* d_src, const uint32_t* d_dst, uint64_t num_entries,
                        uint32_t num_nodes, const kt_schedule* candidates, uint32_t num_candidates,
                        uint32_t repeats, float* ms, kt_schedule* best);
+/* ---- tiled COO/CSR layout (coo2tiledcoocsr, graph.cu:641-706) ---------------------------
+ * The reference's tiled layout of an entry list, built on the device: tile_size =
+ * ceil(num_nodes / tiles_per_dim); entry (s, d) lies in row (s / tile_size * tiles_per_dim +
+ * d / tile_size) * tile_size + s % tile_size; d_tile_src_ptr receives tiles_per_dim^2 * tile_size
+ * + 1 row offsets, d_src_out / d_dst_out the entries ordered by row and, within a row, by
+ * destination.  The engine's own kernels do not read tiles; this serves callers of the reference's
+ * tiled format.  Synchronous. */
+int kt_engine_tiled_coocsr(kt_engine* engine, const uint32_t* d_src, const uint32_t* d_dst, uint64_t num_entries,
+                           uint32_t num_nodes, uint32_t tiles_per_dim, uint32_t* d_tile_src_ptr, uint32_t* d_src_out,
+                           uint32_t* d_dst_out);
+
 /* ---- device-side TSV ingest (replaces createCOOFromFile, graph.cu:37-79) ------------------
  * The same format as kt_read_tsv - "dst src x" triples of unsigned decimal numbers separated by
  * any whitespace, 1-based ids, x ignored - parsed on the device into 0-based entries in the

@@ -209,7 +209,93 @@ int sync_and_check(kt_engine* e) {
     return error_status(e->h_ctrl[kCtrlError]);
 }
 
+// Tiled COO/CSR (coo2tiledcoocsr, graph.cu:641-706): key = row << vb | dst with row =
+// (src / ts * T + dst / ts) * ts + src % ts; the entry index rides along as the value.
+__global__ void k_tile_keys(const uint32_t* __restrict__ src, const uint32_t* __restrict__ dst, uint64_t entries,
+                            uint32_t n, uint32_t T, uint32_t ts, unsigned vb, uint64_t* __restrict__ keys,
+                            uint32_t* __restrict__ ctrl) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t err = 0;
+    if (i < entries) {
+        const uint32_t s = src[i], d = dst[i];
+        if (s >= n || d >= n) {
+            err = kErrBadVertex;
+            keys[i] = 0;
+        } else {
+            const uint64_t row = ((uint64_t)(s / ts) * T + d / ts) * ts + s % ts;
+            keys[i] = (row << vb) | d;
+        }
+    }
+    err = __reduce_or_sync(kFullMask, err);
+    if (err && lane_id() == 0) atomicOr(&ctrl[kCtrlError], err);
+}
+
+// Sorted keys back to entries: the source from the row, the destination from the key.
+__global__ void k_tile_entries(const uint64_t* __restrict__ keys, uint64_t entries, uint32_t T, uint32_t ts,
+                               unsigned vb, uint32_t* __restrict__ src_out, uint32_t* __restrict__ dst_out) {
+    const uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < entries) {
+        const uint64_t key = keys[p];
+        const uint64_t row = key >> vb;
+        const uint64_t tile = row / ts;  // src tile * T + dst tile
+        src_out[p] = (uint32_t)((tile / T) * ts + row % ts);
+        dst_out[p] = (uint32_t)(key & ((1ull << vb) - 1));
+    }
+}
+
+// tile_src_ptr[r] = first sorted position whose row is >= r (rows + 1 offsets).
+__global__ void k_tile_ptr(const uint64_t* __restrict__ keys, uint64_t entries, unsigned vb, uint64_t rows,
+                           uint32_t* __restrict__ ptr) {
+    const uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r > rows) return;
+    uint64_t lo = 0, len = entries;
+    while (len > 0) {
+        const uint64_t half = len >> 1;
+        if ((keys[lo + half] >> vb) < r) {
+            lo += half + 1;
+            len -= half + 1;
+        } else {
+            len = half;
+        }
+    }
+    ptr[r] = (uint32_t)lo;
+}
+
 }  // namespace
+
+int tiled_coocsr(kt_engine* e, const uint32_t* d_src, const uint32_t* d_dst, uint64_t entries, uint32_t n,
+                 uint32_t tiles_per_dim, uint32_t* d_tile_src_ptr, uint32_t* d_src_out, uint32_t* d_dst_out) {
+    if (tiles_per_dim == 0 || n == 0) return fail(KT_ERR_INVALID_ARG, "tiled layout needs tiles_per_dim >= 1 and n >= 1");
+    if (entries >= 0xffffffffull) return fail(KT_ERR_TOO_LARGE, "more than 2^32-2 entries");
+    const uint32_t T = tiles_per_dim;
+    const uint32_t ts = (uint32_t)(((uint64_t)n + T - 1) / T);
+    const uint64_t rows = (uint64_t)T * T * ts;
+    const unsigned vb = bits_for(n > 1 ? n : 2);
+    const unsigned rb = bits_for(rows + 1);
+    if (rb + vb > 64) return fail(KT_ERR_TOO_LARGE, "tiles_per_dim %u too large for %u vertices", T, n);
+    int rc;
+    if ((n > e->cap_nodes || entries > e->cap_entries) &&
+        (rc = reserve(e, n > e->cap_nodes ? n : e->cap_nodes, entries > e->cap_entries ? entries : e->cap_entries)))
+        return rc;
+    cudaStream_t st = e->stream;
+    if ((rc = check_cuda(cudaMemsetAsync(e->ctrl, 0, sizeof(uint32_t) * kCtrlWords, st), "clear control block")))
+        return rc;
+    int in_b = 0;
+    if (entries) {
+        k_tile_keys<<<grid_for(entries), kThreads, 0, st>>>(d_src, d_dst, entries, n, T, ts, vb, e->key_a, e->ctrl);
+        count_launch(e);
+        if ((rc = check_launch(e, "k_tile_keys")) || (rc = sync_and_check(e))) return rc;
+        if ((rc = radix_sort(e, e->key_a, nullptr, e->key_b, nullptr, entries, rb + vb, &in_b))) return rc;
+        k_tile_entries<<<grid_for(entries), kThreads, 0, st>>>(in_b ? e->key_b : e->key_a, entries, T, ts, vb,
+                                                              d_src_out, d_dst_out);
+        count_launch(e);
+        if ((rc = check_launch(e, "k_tile_entries"))) return rc;
+    }
+    k_tile_ptr<<<grid_for(rows + 1), kThreads, 0, st>>>(in_b ? e->key_b : e->key_a, entries, vb, rows, d_tile_src_ptr);
+    count_launch(e);
+    if ((rc = check_launch(e, "k_tile_ptr"))) return rc;
+    return check_cuda(cudaStreamSynchronize(st), "synchronize");
+}
 
 int build_graph(kt_engine* e, const uint32_t* d_src, const uint32_t* d_dst, uint64_t entries, uint32_t n) {
     if (entries & 1) return fail(KT_ERR_NOT_SYMMETRIC, "odd number of entries (%llu): every edge needs both directions",

@@ -437,6 +437,18 @@ int kt_engine_autotune(kt_engine* e, const uint32_t* d_src, const uint32_t* d_ds
     return KT_OK;
 }
 
+int kt_engine_tiled_coocsr(kt_engine* e, const uint32_t* d_src, const uint32_t* d_dst, uint64_t num_entries,
+                           uint32_t num_nodes, uint32_t tiles_per_dim, uint32_t* d_tile_src_ptr, uint32_t* d_src_out,
+                           uint32_t* d_dst_out) {
+    kt::clear_error();
+    if (!e || !d_tile_src_ptr || (num_entries && (!d_src || !d_dst || !d_src_out || !d_dst_out)))
+        return fail(KT_ERR_INVALID_ARG, "kt_engine_tiled_coocsr: null argument");
+    int rc = check_cuda(cudaSetDevice(e->device), "cudaSetDevice");
+    if (rc) return rc;
+    return kt::tiled_coocsr(e, d_src, d_dst, num_entries, num_nodes, tiles_per_dim, d_tile_src_ptr, d_src_out,
+                            d_dst_out);
+}
+
 int kt_engine_set_selector(kt_engine* e, kt_selector* s) {
     kt::clear_error();
     if (!e) return fail(KT_ERR_INVALID_ARG, "kt_engine_set_selector: null engine");

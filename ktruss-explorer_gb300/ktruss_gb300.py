@@ -158,6 +158,8 @@ def lib() -> ctypes.CDLL:
         L.kt_selector_predict.argtypes = [_VP, _FP, ctypes.c_uint32, ctypes.POINTER(Schedule)]
         L.kt_engine_features.argtypes = [_VP, _VP, _VP, ctypes.c_uint64, ctypes.c_uint32, _FP]
         L.kt_engine_set_selector.argtypes = [_VP, _VP]
+        L.kt_engine_tiled_coocsr.argtypes = [_VP, _VP, _VP, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32, _VP,
+                                             _VP, _VP]
         _U64P = ctypes.POINTER(ctypes.c_uint64)
         L.kt_engine_parse_tsv.argtypes = [_VP, _VP, ctypes.c_uint64, _VP, _VP, ctypes.c_uint64, _U64P, _U32P]
         L.kt_engine_read_tsv.argtypes = [_VP, ctypes.c_char_p, _VP, _VP, ctypes.c_uint64, _U64P, _U32P]
@@ -425,6 +427,12 @@ class Engine:
         _check(lib().kt_engine_read_tsv(self._h, os.fsencode(path), d_src, d_dst, capacity, ctypes.byref(ne),
                                         ctypes.byref(nn)))
         return ne.value, nn.value
+
+    def tiled_coocsr(self, d_src: int, d_dst: int, num_entries: int, num_nodes: int, tiles_per_dim: int,
+                     d_tile_src_ptr: int, d_src_out: int, d_dst_out: int) -> None:
+        """The reference's tiled COO/CSR layout of a device entry list (kt_engine_tiled_coocsr)."""
+        _check(lib().kt_engine_tiled_coocsr(self._h, d_src, d_dst, num_entries, num_nodes, tiles_per_dim,
+                                            d_tile_src_ptr, d_src_out, d_dst_out))
 
     def set_selector(self, selector: Optional["Selector"]) -> None:
         """Attach a learned selector (its schedule is used by every decomposition) or detach (None)."""

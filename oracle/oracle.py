@@ -115,3 +115,21 @@ def chain_sample(num_nodes: int, src, dst, budget_s: float) -> dict:
     if rc != 0:
         raise MemoryError("oracle chain sample failed")
     return {"passes": passes.value, "alive_sum": alive.value, "seconds": secs.value}
+
+
+def tiled_coocsr(num_nodes: int, src, dst, tiles_per_dim: int):
+    """Tiled COO/CSR of an entry list, restating coo2tiledcoocsr (graph.cu:641-706) with
+    createEmptyTiledCOOCSR's tile size (graph.cu:574-586): tile_size = ceil(n / T); entry (s, d)
+    belongs to row (s // tile_size * T + d // tile_size) * tile_size + s % tile_size; rows are
+    binned in entry order and each row's destinations sorted ascending.  Returns (tile_src_ptr with
+    T*T*tile_size + 1 offsets, src, dst)."""
+    src, dst = _u32(src).astype(np.int64), _u32(dst).astype(np.int64)
+    T = int(tiles_per_dim)
+    ts = (num_nodes + T - 1) // T
+    rows = T * T * ts
+    tile_src = (src // ts * T + dst // ts) * ts + src % ts
+    ptr = np.zeros(rows + 1, np.int64)
+    np.add.at(ptr, tile_src + 1, 1)
+    ptr = np.cumsum(ptr)
+    order = np.lexsort((dst, tile_src))  # by row, then destination (rows hold one source each)
+    return ptr.astype(np.uint32), src[order].astype(np.uint32), dst[order].astype(np.uint32)
