@@ -226,6 +226,14 @@ int kt_engine_decompose(kt_engine* engine, const uint32_t* d_src, const uint32_t
 int kt_engine_ktruss(kt_engine* engine, const uint32_t* d_src, const uint32_t* d_dst,
                      uint64_t num_entries, uint32_t num_nodes, uint32_t k, uint8_t* d_keep,
                      int sync);
+/* Repeats the engine's last successful kt_engine_decompose or kt_engine_ktruss call on the same
+ * device buffers, whose contents the caller has left unchanged: the reference's repeat runs
+ * (-w/-x, kernel_ddc.cu:227-244), which rebuild the graph and run the whole k-truss again.  The
+ * first replay captures the call's device pipeline (build, support count, peel, output) into a
+ * CUDA graph without the input checks the call already made; later replays launch that graph.
+ * A different call, a new schedule or selector, or a larger reservation drops the graph.
+ * Statistics afterwards: everything but the per-phase times (0); last_ms is the replay's. */
+int kt_engine_replay(kt_engine* engine, int sync);
 /* Batched decomposition (no counterpart in the reference): num_graphs graphs in one call, given
  * as one COO over disjoint vertex ranges — graph g owns vertices [d_vertex_offsets[g],
  * d_vertex_offsets[g+1]), num_graphs+1 offsets ending at num_nodes, and every entry stays inside

@@ -99,6 +99,27 @@ size_t carve(kt_engine* e, char* base, uint32_t n, uint64_t N, bool staging) {
     return c.off;
 }
 
+void drop_replay(kt_engine* e) {
+    if (e->replay) cudaGraphExecDestroy(e->replay);
+    e->replay = nullptr;
+    e->replay_direct = false;
+}
+
+// Records a successful device-buffer call for kt_engine_replay; a different call drops the
+// captured pipeline of the previous one.
+void remember(kt_engine* e, const kt_engine::LastCall& c) {
+    const kt_engine::LastCall& l = e->last;
+    if (l.kind != c.kind || l.src != c.src || l.dst != c.dst || l.entries != c.entries || l.n != c.n ||
+        l.truss != c.truss || l.k_max != c.k_max || l.k != c.k || l.keep != c.keep)
+        drop_replay(e);
+    e->last = c;
+}
+
+void forget(kt_engine* e) {
+    drop_replay(e);
+    e->last = kt_engine::LastCall{};
+}
+
 int reserve(kt_engine* e, uint32_t max_nodes, uint64_t max_entries) {
     if (max_nodes <= e->cap_nodes && max_entries <= e->cap_entries && e->arena) return KT_OK;
     max_nodes = std::max(max_nodes, e->cap_nodes);
@@ -107,6 +128,7 @@ int reserve(kt_engine* e, uint32_t max_nodes, uint64_t max_entries) {
     if (rc) return rc;
     if (e->arena) {
         if ((rc = check_cuda(cudaStreamSynchronize(e->stream), "synchronize before resize"))) return rc;
+        drop_replay(e);  // the captured pipeline points into the old workspace
         cudaFree(e->arena);
         e->arena = nullptr;
         e->arena_bytes = 0;
@@ -222,6 +244,73 @@ int run_ktruss(kt_engine* e, const uint32_t* d_src, const uint32_t* d_dst, uint6
     return fill_graph_stats(e);
 }
 
+// The device pipeline of the remembered call, for a trusted run (its input passed the checks
+// of the call itself): no host reads, so it can be captured into a CUDA graph.
+int replay_pipeline(kt_engine* e) {
+    const kt_engine::LastCall& c = e->last;
+    int rc;
+    if ((rc = kt::build_graph(e, c.src, c.dst, c.entries, c.n))) return rc;
+    if (c.kind == 1)
+        return (rc = kt::count_support(e)) || (rc = kt::peel_decompose(e)) ||
+                       (rc = kt::emit_truss_per_entry(e, c.truss, c.k_max))
+                   ? rc
+                   : KT_OK;
+    if (c.k >= 3 && (rc = kt::count_support(e))) return rc;
+    if ((rc = kt::peel_single_k(e, c.k)) || (rc = kt::emit_keep(e, c.keep))) return rc;
+    return KT_OK;
+}
+
+// Captures the remembered call's pipeline once (CUDA graph; if the capture is refused, later
+// replays launch the pipeline directly), then launches it between the start and stop events.
+int replay(kt_engine* e, int sync) {
+    if (!e->last.kind) return fail(KT_ERR_INVALID_ARG, "kt_engine_replay: no decomposition or single-k call to repeat");
+    int rc;
+    if (!e->replay && !e->replay_direct) {
+        const uint64_t l0 = e->launches;
+        cudaGraph_t g = nullptr;
+        e->trusted = true;
+        rc = check_cuda(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+        if (!rc) {
+            const int body = replay_pipeline(e);
+            const cudaError_t end = cudaStreamEndCapture(e->stream, &g);
+            rc = body ? body : check_cuda(end, "capture the pipeline");
+        }
+        e->trusted = false;
+        e->replay_launches = e->launches - l0;
+        e->launches = l0;
+        e->replay_peel_mode = e->peel_mode;
+        if (!rc) rc = check_cuda(cudaGraphInstantiate(&e->replay, g, 0), "instantiate the pipeline graph");
+        if (g) cudaGraphDestroy(g);
+        if (rc) {
+            // capture errors leave the context usable: fall back to direct launches
+            (void)cudaGetLastError();
+            kt::clear_error();
+            e->replay = nullptr;
+            e->replay_direct = true;
+        }
+    }
+    if ((rc = record_start(e))) return rc;
+    if (e->replay_direct) {
+        e->trusted = true;
+        rc = replay_pipeline(e);
+        e->trusted = false;
+        if (rc) return rc;
+    } else {
+        if ((rc = check_cuda(cudaGraphLaunch(e->replay, e->stream), "launch the pipeline graph"))) return rc;
+        e->launches += e->replay_launches;
+    }
+    if ((rc = check_cuda(cudaEventRecord(e->ev_stop, e->stream), "record stop"))) return rc;
+    e->peel_mode = e->replay_peel_mode;
+    e->peel_timed = false;
+    e->stats_ready = false;
+    e->stats.build_ms = e->stats.select_ms = e->stats.support_ms = e->stats.peel_ms = 0;
+    e->replay_timing = true;
+    fill_graph_stats(e);
+    if (!sync) return KT_OK;
+    if ((rc = check_cuda(cudaStreamSynchronize(e->stream), "synchronize"))) return rc;
+    return kt::finish_stats(e);
+}
+
 int check_coo(const kt_coo* g, const char* what) {
     if (!g) return fail(KT_ERR_INVALID_ARG, "%s: null graph", what);
     if (g->num_edges && (!g->src_idx || !g->dst_idx)) return fail(KT_ERR_INVALID_ARG, "%s: null edge arrays", what);
@@ -268,6 +357,7 @@ int kt_engine_destroy(kt_engine* e) {
     if (!e) return KT_OK;
     cudaSetDevice(e->device);
     if (e->stream) cudaStreamSynchronize(e->stream);
+    kt::drop_replay(e);
     if (e->arena) cudaFree(e->arena);
     if (e->aux) cudaFree(e->aux);
     if (e->ctrl) cudaFree(e->ctrl);
@@ -301,7 +391,13 @@ int kt_engine_decompose(kt_engine* e, const uint32_t* d_src, const uint32_t* d_d
     kt::clear_error();
     int rc = check_cuda(cudaSetDevice(e->device), "cudaSetDevice");
     if (rc) return rc;
-    if ((rc = run_decompose(e, d_src, d_dst, num_entries, num_nodes, d_truss, d_k_max))) return rc;
+    if ((rc = run_decompose(e, d_src, d_dst, num_entries, num_nodes, d_truss, d_k_max))) {
+        kt::forget(e);  // only a call that passed its checks is repeated
+        return rc;
+    }
+    kt_engine::LastCall c;
+    c.kind = 1, c.src = d_src, c.dst = d_dst, c.entries = num_entries, c.n = num_nodes, c.truss = d_truss, c.k_max = d_k_max;
+    kt::remember(e, c);
     if (sync) {
         if ((rc = check_cuda(cudaStreamSynchronize(e->stream), "synchronize"))) return rc;
         return kt::finish_stats(e);
@@ -316,12 +412,26 @@ int kt_engine_ktruss(kt_engine* e, const uint32_t* d_src, const uint32_t* d_dst,
     kt::clear_error();
     int rc = check_cuda(cudaSetDevice(e->device), "cudaSetDevice");
     if (rc) return rc;
-    if ((rc = run_ktruss(e, d_src, d_dst, num_entries, num_nodes, k, d_keep))) return rc;
+    if ((rc = run_ktruss(e, d_src, d_dst, num_entries, num_nodes, k, d_keep))) {
+        kt::forget(e);
+        return rc;
+    }
+    kt_engine::LastCall c;
+    c.kind = 2, c.src = d_src, c.dst = d_dst, c.entries = num_entries, c.n = num_nodes, c.k = k, c.keep = d_keep;
+    kt::remember(e, c);
     if (sync) {
         if ((rc = check_cuda(cudaStreamSynchronize(e->stream), "synchronize"))) return rc;
         return kt::finish_stats(e);
     }
     return KT_OK;
+}
+
+int kt_engine_replay(kt_engine* e, int sync) {
+    if (!e) return fail(KT_ERR_INVALID_ARG, "kt_engine_replay: null engine");
+    kt::clear_error();
+    int rc = check_cuda(cudaSetDevice(e->device), "cudaSetDevice");
+    if (rc) return rc;
+    return replay(e, sync);
 }
 
 kt_schedule kt_schedule_default(void) { return kt_schedule{8, 32, 85, 50, 0}; }
@@ -339,6 +449,7 @@ int kt_engine_set_schedule(kt_engine* e, const kt_schedule* s) {
         return fail(KT_ERR_INVALID_ARG, "recount_percent must be 0..100 (got %u)", s->recount_percent);
     if (s->peel_blocks > 2) return fail(KT_ERR_INVALID_ARG, "peel_blocks must be 0, 1 or 2 (got %u)", s->peel_blocks);
     e->sched = *s;
+    kt::drop_replay(e);  // a replay captures the pipeline again with this schedule
     return KT_OK;
 }
 
@@ -395,6 +506,7 @@ int kt_engine_autotune(kt_engine* e, const uint32_t* d_src, const uint32_t* d_ds
     if (!e) return fail(KT_ERR_INVALID_ARG, "kt_engine_autotune: null engine");
     if (num_entries && (!d_src || !d_dst)) return fail(KT_ERR_INVALID_ARG, "kt_engine_autotune: null buffer");
     if (repeats == 0) return fail(KT_ERR_INVALID_ARG, "kt_engine_autotune: repeats must be >= 1");
+    kt::forget(e);
     kt_schedule grid[36];
     if (!candidates) {
         num_candidates = kt_schedule_grid(grid, 36);
@@ -453,6 +565,7 @@ int kt_engine_set_selector(kt_engine* e, kt_selector* s) {
     kt::clear_error();
     if (!e) return fail(KT_ERR_INVALID_ARG, "kt_engine_set_selector: null engine");
     e->selector = s;
+    kt::drop_replay(e);
     return KT_OK;
 }
 
@@ -539,6 +652,7 @@ int kt_engine_decompose_batch(kt_engine* e, const uint32_t* d_src, const uint32_
     int rc = check_cuda(cudaSetDevice(e->device), "cudaSetDevice");
     if (rc) return rc;
     // the union of disjoint graphs: its truss numbers are each graph's own
+    kt::forget(e);
     e->batch_call = true;
     rc = run_decompose(e, d_src, d_dst, num_entries, num_nodes, d_truss_per_entry, nullptr);
     e->batch_call = false;
@@ -571,6 +685,7 @@ int kt_decompose_batch(const uint32_t* src, const uint32_t* dst, uint64_t num_en
     int rc;
     if ((rc = default_engine(&e))) return rc;
     std::lock_guard<std::mutex> lock(g_default_mu);
+    kt::forget(e);  // host-buffer calls overwrite the staging buffers a replay would read
     if ((rc = check_cuda(cudaSetDevice(e->device), "cudaSetDevice"))) return rc;
     if ((rc = kt::reserve(e, std::max(num_nodes, e->cap_nodes), std::max(num_entries, e->cap_entries)))) return rc;
     const size_t need = 2 * (size_t)num_graphs + 1;
@@ -620,6 +735,7 @@ int kt_decompose(const kt_coo* graph, uint32_t* truss_per_entry, uint32_t* k_max
     kt_engine* e = nullptr;
     if ((rc = default_engine(&e))) return rc;
     std::lock_guard<std::mutex> lock(g_default_mu);
+    kt::forget(e);  // host-buffer calls overwrite the staging buffers a replay would read
     if ((rc = check_cuda(cudaSetDevice(e->device), "cudaSetDevice"))) return rc;
     const uint64_t N = graph->num_edges;
     if ((rc = kt::reserve(e, std::max(graph->num_nodes, e->cap_nodes), std::max(N, e->cap_entries)))) return rc;
@@ -656,6 +772,7 @@ int kt_ktruss(const kt_coo* graph, kt_coo* truss, const kt_config* config) {
     kt_engine* e = nullptr;
     if ((rc = default_engine(&e))) return rc;
     std::lock_guard<std::mutex> lock(g_default_mu);
+    kt::forget(e);  // host-buffer calls overwrite the staging buffers a replay would read
     if ((rc = check_cuda(cudaSetDevice(e->device), "cudaSetDevice"))) return rc;
     const uint64_t N = graph->num_edges;
     const int verbose = config->verbosity >= 1;
@@ -671,10 +788,19 @@ int kt_ktruss(const kt_coo* graph, kt_coo* truss, const kt_config* config) {
     // -w warm-up and -x timed runs (kernel_ddc.cu:227-244); each run rebuilds the graph from
     // the input entries, so every run is the full device pipeline.
     const uint32_t runs = config->num_warmup_runs + config->num_timed_runs;
+    // Runs after the first repeat it on the same input: kt_engine_replay's CUDA graph.
     for (uint32_t i = 0; i < (runs ? runs : 1); ++i) {
         if (verbose) printf("    Performing K-truss\n");
-        if ((rc = run_ktruss(e, e->in_src, e->in_dst, N, graph->num_nodes, config->k, e->out_u8))) return rc;
-        if ((rc = kt::finish_stats(e))) return rc;
+        if (i == 0) {
+            if ((rc = run_ktruss(e, e->in_src, e->in_dst, N, graph->num_nodes, config->k, e->out_u8))) return rc;
+            kt_engine::LastCall c;
+            c.kind = 2, c.src = e->in_src, c.dst = e->in_dst, c.entries = N, c.n = graph->num_nodes, c.k = config->k,
+            c.keep = e->out_u8;
+            kt::remember(e, c);
+            if ((rc = kt::finish_stats(e))) return rc;
+        } else if ((rc = replay(e, 1))) {
+            return rc;
+        }
         if (config->verbosity == 0 && i >= config->num_warmup_runs) {
             kt_print_config_csv(config);
             printf("%f ms\n", e->stats.last_ms);

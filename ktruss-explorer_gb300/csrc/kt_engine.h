@@ -95,6 +95,26 @@ struct kt_engine {
     uint32_t* sel_choice = nullptr;    // the selector's schedule index
     kt_stats stats{};
     int peel_mode = 0;          // 0 decomposition, 1 single-k
+    // Replay (kt_engine_replay): the last decomposition or single-k call on device buffers, and
+    // its device pipeline as an instantiated CUDA graph once captured.  `trusted` marks a pipeline
+    // run whose input already passed its checks: no host reads, no timing events (capturable).
+    struct LastCall {
+        int kind = 0;  // 0 none, 1 decomposition, 2 single-k truss
+        const uint32_t* src = nullptr;
+        const uint32_t* dst = nullptr;
+        uint64_t entries = 0;
+        uint32_t n = 0;
+        uint32_t* truss = nullptr;
+        uint32_t* k_max = nullptr;
+        uint32_t k = 0;
+        uint8_t* keep = nullptr;
+    } last;
+    cudaGraphExec_t replay = nullptr;
+    bool replay_direct = false;      // the pipeline could not be captured: replays launch it directly
+    uint64_t replay_launches = 0;    // kernel launches in one replay
+    int replay_peel_mode = 0;
+    bool trusted = false;
+    bool replay_timing = false;      // last_ms of a replay is read when the stream has drained
     bool stats_ready = false;   // stats already read back from the device
 };
 
@@ -106,6 +126,10 @@ int check_cuda(cudaError_t err, const char* what);
 int check_launch(kt_engine* e, const char* what);
 
 int reserve(kt_engine* e, uint32_t max_nodes, uint64_t max_entries);
+// kt_engine_replay bookkeeping (kt_engine.cu)
+void drop_replay(kt_engine* e);
+void remember(kt_engine* e, const kt_engine::LastCall& c);
+void forget(kt_engine* e);
 size_t carve(kt_engine* e, char* base, uint32_t n, uint64_t N, bool staging);
 
 // kt_sort.cu

@@ -787,7 +787,7 @@ int launch_peel(kt_engine* e, uint32_t single_k) {
     P.single_k = single_k;
     P.timeout_ns = kPeelTimeoutNs;
     void* args[] = {&P};
-    const bool timed = e->ev_peel0 && e->ev_peel1;
+    const bool timed = e->ev_peel0 && e->ev_peel1 && !e->trusted;
     if (timed && (rc = check_cuda(cudaEventRecord(e->ev_peel0, e->stream), "record event"))) return rc;
     const int blocks_per_sm = wide && per_sm >= 2 ? 2 : 1;
     rc = check_cuda(cudaLaunchCooperativeKernel(kernel, dim3((unsigned)(e->num_sms * blocks_per_sm)),
@@ -885,6 +885,11 @@ int emit_keep(kt_engine* e, uint8_t* d_keep) {
 // one pass each.
 int finish_stats(kt_engine* e) {
     if (e->stats_ready) return KT_OK;
+    if (e->replay_timing) {  // the stream has drained: the replay's events are complete
+        e->replay_timing = false;
+        int rc = check_cuda(cudaEventElapsedTime(&e->stats.last_ms, e->ev_start, e->ev_stop), "elapsed time");
+        if (rc) return rc;
+    }
     if (e->m == 0 || e->peel_mode == 2) {
         e->stats.compactions = 0;
         e->stats.walk_entries = 0;

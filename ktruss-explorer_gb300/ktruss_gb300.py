@@ -131,6 +131,7 @@ def lib() -> ctypes.CDLL:
         L.kt_engine_decompose.argtypes = [_VP, _VP, _VP, ctypes.c_uint64, ctypes.c_uint32, _VP, _VP, ctypes.c_int]
         L.kt_engine_ktruss.argtypes = [_VP, _VP, _VP, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32, _VP,
                                        ctypes.c_int]
+        L.kt_engine_replay.argtypes = [_VP, ctypes.c_int]
         L.kt_engine_stats.argtypes = [_VP, ctypes.POINTER(Stats)]
         L.kt_last_stats.argtypes = [ctypes.POINTER(Stats)]
         L.kt_engine_selftest_barrier_timeout.argtypes = [_VP, ctypes.c_uint64]
@@ -384,6 +385,11 @@ class Engine:
                sync: bool = True) -> None:
         _check(lib().kt_engine_ktruss(self._h, d_src, d_dst, num_entries, num_nodes, k & 0xFFFFFFFF, d_keep,
                                       int(sync)))
+
+    def replay(self, sync: bool = True) -> None:
+        """Repeats the last decompose/ktruss call on the same (unchanged) device buffers through
+        a CUDA graph of its device pipeline, captured at the first replay."""
+        _check(lib().kt_engine_replay(self._h, int(sync)))
 
     def set_schedule(self, support_group: int = 8, chunk_width: int = 32, compact_percent: int = 85,
                      recount_percent: int = 50, peel_blocks: int = 0) -> None:
