@@ -73,12 +73,15 @@ __global__ void k_rank_scatter(const uint64_t* __restrict__ sorted, uint32_t n, 
     }
 }
 
+// An id >= n (already flagged by k_degree; the call fails at the end of the build) is read as
+// vertex 0, so that every kernel up to that check indexes inside its arrays.
 __global__ void k_edge_keys(const uint32_t* __restrict__ src, const uint32_t* __restrict__ dst, uint64_t entries,
-                            const uint32_t* __restrict__ rank, unsigned vb, uint64_t* __restrict__ keys,
+                            uint32_t n, const uint32_t* __restrict__ rank, unsigned vb, uint64_t* __restrict__ keys,
                             uint32_t* __restrict__ vals) {
     uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < entries) {
-        keys[i] = ((uint64_t)rank[src[i]] << vb) | rank[dst[i]];
+        const uint32_t s = src[i], d = dst[i];
+        keys[i] = ((uint64_t)rank[s < n ? s : 0] << vb) | rank[d < n ? d : 0];
         vals[i] = (uint32_t)i;
     }
 }
@@ -140,18 +143,26 @@ __global__ void k_orient(const uint64_t* __restrict__ keys, uint64_t entries, un
 }
 
 // Lower-rank entries (row r, column c < r) take the id of edge (c, r) from c's oriented row.
-__global__ void k_in_eid(const uint64_t* __restrict__ keys, uint64_t entries, unsigned vb,
+// The oriented CSR must hold exactly m = entries / 2 edges; an input that is not symmetric can
+// leave rows that do not nest in [0, m): they are flagged, never searched.
+__global__ void k_in_eid(const uint64_t* __restrict__ keys, uint64_t entries, unsigned vb, uint32_t n, uint32_t m,
                          const uint32_t* __restrict__ o_ptr, const uint32_t* __restrict__ o_col,
                          uint32_t* __restrict__ s_eid, uint32_t* __restrict__ ctrl) {
     uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     uint32_t err = 0;
+    if (p == 0 && o_ptr[n] != m) err = kErrAsymmetric;
     if (p < entries) {
         uint64_t key = keys[p];
         uint32_t row = (uint32_t)(key >> vb), col = (uint32_t)(key & ((1ull << vb) - 1));
         if (col < row) {
-            uint32_t lo = o_ptr[col], len = o_ptr[col + 1] - lo;
-            uint32_t idx = lower_bound_u32(o_col + lo, len, row);
-            if (idx < len && o_col[lo + idx] == row) s_eid[p] = lo + idx;
+            const uint32_t lo = o_ptr[col], hi = o_ptr[col + 1];
+            uint32_t idx = 0xffffffffu;
+            if (lo <= hi && hi <= m) {
+                const uint32_t len = hi - lo;
+                idx = lower_bound_u32(o_col + lo, len, row);
+                if (idx >= len || o_col[lo + idx] != row) idx = 0xffffffffu;
+            }
+            if (idx != 0xffffffffu) s_eid[p] = lo + idx;
             else { s_eid[p] = 0; err = kErrAsymmetric; }
         }
     }
@@ -323,7 +334,8 @@ int build_graph(kt_engine* e, const uint32_t* d_src, const uint32_t* d_dst, uint
         count_launch(e);
         if ((rc = check_launch(e, "k_degree"))) return rc;
     }
-    if (!e->trusted && (rc = sync_and_check(e))) return rc;
+    // (input errors are read back once, at the end of the build: every kernel before that
+    // check indexes inside its arrays whatever the input)
 
     // 2. ranks: ascending (degree, id)
     k_rank_keys<<<grid_for(n), kThreads, 0, st>>>(e->deg, n, vb, e->key_a);
@@ -340,7 +352,8 @@ int build_graph(kt_engine* e, const uint32_t* d_src, const uint32_t* d_dst, uint
 
     // 3. sort entries by (rank[src], rank[dst])
     if (entries) {
-        k_edge_keys<<<grid_for(entries), kThreads, 0, st>>>(d_src, d_dst, entries, e->rank, vb, e->key_a, e->val_a);
+        k_edge_keys<<<grid_for(entries), kThreads, 0, st>>>(d_src, d_dst, entries, n, e->rank, vb, e->key_a,
+                                                            e->val_a);
         count_launch(e);
         if ((rc = check_launch(e, "k_edge_keys"))) return rc;
         if ((rc = radix_sort(e, e->key_a, e->val_a, e->key_b, e->val_b, entries, 2 * vb, &in_b))) return rc;
@@ -368,20 +381,9 @@ int build_graph(kt_engine* e, const uint32_t* d_src, const uint32_t* d_dst, uint
         count_launch(e);
         if ((rc = check_launch(e, "k_orient"))) return rc;
     }
-    // the oriented CSR must hold exactly half the entries before its rows are searched (a
-    // trusted run repeats an input that passed these checks)
-    if (!e->trusted) {
-        uint32_t m_out = 0;
-        if ((rc = check_cuda(cudaMemcpyAsync(&m_out, e->o_ptr + n, sizeof(uint32_t), cudaMemcpyDeviceToHost, st),
-                             "read edge count")))
-            return rc;
-        if ((rc = sync_and_check(e))) return rc;
-        if (m_out != e->m)
-            return fail(KT_ERR_NOT_SYMMETRIC, "%u entries point to higher-degree-rank vertices, %u to lower ones",
-                        m_out, (uint32_t)(entries - m_out));
-    }
     if (entries) {
-        k_in_eid<<<grid_for(entries), kThreads, 0, st>>>(keys, entries, vb, e->o_ptr, e->o_col, e->s_eid, e->ctrl);
+        k_in_eid<<<grid_for(entries), kThreads, 0, st>>>(keys, entries, vb, n, e->m, e->o_ptr, e->o_col, e->s_eid,
+                                                         e->ctrl);
         count_launch(e);
         if ((rc = check_launch(e, "k_in_eid"))) return rc;
         k_entry_eid<<<grid_for(entries), kThreads, 0, st>>>(e->sorted_entry, e->s_eid, entries, e->entry_eid);
