@@ -286,6 +286,17 @@ uint32_t kt_schedule_grid(kt_schedule* out, uint32_t cap);
 int kt_engine_autotune(kt_engine* engine, const uint32_t* d_src, const uint32_t* d_dst, uint64_t num_entries,
                        uint32_t num_nodes, const kt_schedule* candidates, uint32_t num_candidates,
                        uint32_t repeats, float* ms, kt_schedule* best);
+/* ---- symmetrize and deduplicate ----------------------------------------------------------
+ * Turns an arbitrary entry list on the device (one or both directions, duplicates, self loops)
+ * into the symmetric simple graph the k-truss calls take: each undirected edge {u, v}, u != v,
+ * once as (min, max) in sorted order at positions [0, u), then reversed at [u, 2u).  *num_out =
+ * 2u; KT_ERR_CAPACITY (nothing written) if 2u > capacity; KT_ERR_INVALID_ARG for an id >=
+ * num_nodes.  The reference's reader requires files that already list both directions
+ * (graph.cu:37-79); this is the device-side sort and dedup for inputs that do not.  Synchronous. */
+int kt_engine_symmetrize(kt_engine* engine, const uint32_t* d_src, const uint32_t* d_dst, uint64_t num_entries,
+                         uint32_t num_nodes, uint32_t* d_src_out, uint32_t* d_dst_out, uint64_t capacity,
+                         uint64_t* num_out);
+
 /* ---- tiled COO/CSR layout (coo2tiledcoocsr, graph.cu:641-706) ---------------------------
  * The reference's tiled layout of an entry list, built on the device: tile_size =
  * ceil(num_nodes / tiles_per_dim); entry (s, d) lies in row (s / tile_size * tiles_per_dim +

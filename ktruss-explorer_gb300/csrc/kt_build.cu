@@ -272,7 +272,96 @@ __global__ void k_tile_ptr(const uint64_t* __restrict__ keys, uint64_t entries, 
     ptr[r] = (uint32_t)lo;
 }
 
+// Symmetrize and deduplicate: entry i becomes the undirected key (min << vb | max); ids >= n
+// set kErrBadVertex (key 0, a self loop, dropped).
+__global__ void k_canon_keys(const uint32_t* __restrict__ src, const uint32_t* __restrict__ dst, uint64_t entries,
+                             uint32_t n, unsigned vb, uint64_t* __restrict__ keys, uint32_t* __restrict__ ctrl) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t err = 0;
+    if (i < entries) {
+        const uint32_t s = src[i], d = dst[i];
+        if (s >= n || d >= n) {
+            err = kErrBadVertex;
+            keys[i] = 0;
+        } else {
+            keys[i] = ((uint64_t)(s < d ? s : d) << vb) | (s < d ? d : s);
+        }
+    }
+    err = __reduce_or_sync(kFullMask, err);
+    if (err && lane_id() == 0) atomicOr(&ctrl[kCtrlError], err);
+}
+
+// flag[p] = 1 for the first copy of each sorted key that is not a self loop; flag[entries] = 0.
+__device__ __forceinline__ bool canon_first(const uint64_t* keys, uint64_t p, unsigned vb) {
+    const uint64_t key = keys[p];
+    return (key >> vb) != (key & ((1ull << vb) - 1)) && (p == 0 || keys[p - 1] != key);
+}
+
+__global__ void k_canon_flags(const uint64_t* __restrict__ keys, uint64_t entries, unsigned vb,
+                              uint32_t* __restrict__ flag) {
+    const uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < entries) flag[p] = canon_first(keys, p, vb) ? 1u : 0u;
+    else if (p == entries) flag[p] = 0;
+}
+
+// Unique edge j (pos[p] after the scan) goes to j as (lo, hi) and to u + j as (hi, lo), where
+// u = pos[entries]; nothing is written unless all 2u entries fit.
+__global__ void k_canon_emit(const uint64_t* __restrict__ keys, uint64_t entries, unsigned vb,
+                             const uint32_t* __restrict__ pos, uint64_t capacity, uint32_t* __restrict__ src_out,
+                             uint32_t* __restrict__ dst_out) {
+    const uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const uint64_t u = pos[entries];
+    if (p >= entries || 2 * u > capacity || !canon_first(keys, p, vb)) return;
+    const uint64_t key = keys[p];
+    const uint32_t lo = (uint32_t)(key >> vb), hi = (uint32_t)(key & ((1ull << vb) - 1));
+    const uint64_t j = pos[p];
+    src_out[j] = lo;
+    dst_out[j] = hi;
+    src_out[u + j] = hi;
+    dst_out[u + j] = lo;
+}
+
 }  // namespace
+
+int symmetrize(kt_engine* e, const uint32_t* d_src, const uint32_t* d_dst, uint64_t entries, uint32_t n,
+               uint32_t* d_src_out, uint32_t* d_dst_out, uint64_t capacity, uint64_t* num_out) {
+    *num_out = 0;
+    if (entries >= 0xffffffffull) return fail(KT_ERR_TOO_LARGE, "more than 2^32-2 entries");
+    if (entries && n == 0) return fail(KT_ERR_INVALID_ARG, "entries given for a graph with 0 vertices");
+    if (entries == 0) return KT_OK;
+    int rc;
+    if ((n > e->cap_nodes || entries > e->cap_entries) &&
+        (rc = reserve(e, n > e->cap_nodes ? n : e->cap_nodes, entries > e->cap_entries ? entries : e->cap_entries)))
+        return rc;
+    cudaStream_t st = e->stream;
+    const unsigned vb = bits_for(n > 1 ? n : 2);
+    if ((rc = check_cuda(cudaMemsetAsync(e->ctrl, 0, sizeof(uint32_t) * kCtrlWords, st), "clear control block")))
+        return rc;
+    k_canon_keys<<<grid_for(entries), kThreads, 0, st>>>(d_src, d_dst, entries, n, vb, e->key_a, e->ctrl);
+    count_launch(e);
+    if ((rc = check_launch(e, "k_canon_keys"))) return rc;
+    int in_b = 0;
+    if ((rc = radix_sort(e, e->key_a, nullptr, e->key_b, nullptr, entries, 2 * vb, &in_b))) return rc;
+    const uint64_t* keys = in_b ? e->key_b : e->key_a;
+    // the other key buffer (2 * entries words) holds the flags and, scanned in place, the positions
+    uint32_t* pos = reinterpret_cast<uint32_t*>(in_b ? e->key_a : e->key_b);
+    k_canon_flags<<<grid_for(entries + 1), kThreads, 0, st>>>(keys, entries, vb, pos);
+    count_launch(e);
+    if ((rc = check_launch(e, "k_canon_flags")) || (rc = exclusive_scan(e, pos, pos, entries + 1))) return rc;
+    k_canon_emit<<<grid_for(entries), kThreads, 0, st>>>(keys, entries, vb, pos, capacity, d_src_out, d_dst_out);
+    count_launch(e);
+    if ((rc = check_launch(e, "k_canon_emit"))) return rc;
+    uint32_t u = 0;
+    if ((rc = check_cuda(cudaMemcpyAsync(&u, pos + entries, sizeof(uint32_t), cudaMemcpyDeviceToHost, st),
+                         "read edge count")) ||
+        (rc = sync_and_check(e)))
+        return rc;
+    *num_out = 2ull * u;
+    if (2ull * u > capacity)
+        return fail(KT_ERR_CAPACITY, "symmetrized graph has %llu entries, capacity %llu", 2ull * u,
+                    (unsigned long long)capacity);
+    return KT_OK;
+}
 
 int tiled_coocsr(kt_engine* e, const uint32_t* d_src, const uint32_t* d_dst, uint64_t entries, uint32_t n,
                  uint32_t tiles_per_dim, uint32_t* d_tile_src_ptr, uint32_t* d_src_out, uint32_t* d_dst_out) {

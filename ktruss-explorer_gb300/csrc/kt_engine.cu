@@ -49,7 +49,7 @@ size_t carve(kt_engine* e, char* base, uint32_t n, uint64_t N, bool staging) {
     const uint64_t keys = std::max<uint64_t>(N, n);
     const uint64_t sort_blocks = (keys + 2047) / 2048;
     const uint64_t hist_words = 256 * sort_blocks;
-    const uint64_t scan_max = std::max<uint64_t>((uint64_t)n + 1, hist_words);
+    const uint64_t scan_max = std::max<uint64_t>(std::max<uint64_t>((uint64_t)n, N) + 1, hist_words);
     const uint64_t scan_words = scan_max / 4096 + 4096;
     Carver c{base};
     e->key_a = c.take<uint64_t>(keys);
@@ -559,6 +559,17 @@ int kt_engine_tiled_coocsr(kt_engine* e, const uint32_t* d_src, const uint32_t* 
     if (rc) return rc;
     return kt::tiled_coocsr(e, d_src, d_dst, num_entries, num_nodes, tiles_per_dim, d_tile_src_ptr, d_src_out,
                             d_dst_out);
+}
+
+int kt_engine_symmetrize(kt_engine* e, const uint32_t* d_src, const uint32_t* d_dst, uint64_t num_entries,
+                         uint32_t num_nodes, uint32_t* d_src_out, uint32_t* d_dst_out, uint64_t capacity,
+                         uint64_t* num_out) {
+    kt::clear_error();
+    if (!e || !num_out || (num_entries && (!d_src || !d_dst || (capacity && (!d_src_out || !d_dst_out)))))
+        return fail(KT_ERR_INVALID_ARG, "kt_engine_symmetrize: null argument");
+    int rc = check_cuda(cudaSetDevice(e->device), "cudaSetDevice");
+    if (rc) return rc;
+    return kt::symmetrize(e, d_src, d_dst, num_entries, num_nodes, d_src_out, d_dst_out, capacity, num_out);
 }
 
 int kt_engine_set_selector(kt_engine* e, kt_selector* s) {

@@ -143,6 +143,11 @@ int radix_sort(kt_engine* e, uint64_t* key_a, uint32_t* val_a, uint64_t* key_b, 
 // kt_build.cu: relabel by degree, orient, sort, symmetric + oriented CSR, edge ids.
 int build_graph(kt_engine* e, const uint32_t* d_src, const uint32_t* d_dst, uint64_t entries, uint32_t n);
 
+// Symmetric simple graph of an arbitrary entry list (directions merged, duplicates and self loops
+// dropped): (lo, hi) pairs in sorted order, then the same pairs reversed; synchronous.
+int symmetrize(kt_engine* e, const uint32_t* d_src, const uint32_t* d_dst, uint64_t entries, uint32_t n,
+               uint32_t* d_src_out, uint32_t* d_dst_out, uint64_t capacity, uint64_t* num_out);
+
 // Tiled COO/CSR of an entry list (the reference's tiled layout); synchronous.
 int tiled_coocsr(kt_engine* e, const uint32_t* d_src, const uint32_t* d_dst, uint64_t entries, uint32_t n,
                  uint32_t tiles_per_dim, uint32_t* d_tile_src_ptr, uint32_t* d_src_out, uint32_t* d_dst_out);

@@ -161,6 +161,8 @@ def lib() -> ctypes.CDLL:
         L.kt_engine_set_selector.argtypes = [_VP, _VP]
         L.kt_engine_tiled_coocsr.argtypes = [_VP, _VP, _VP, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32, _VP,
                                              _VP, _VP]
+        L.kt_engine_symmetrize.argtypes = [_VP, _VP, _VP, ctypes.c_uint64, ctypes.c_uint32, _VP, _VP, ctypes.c_uint64,
+                                           ctypes.POINTER(ctypes.c_uint64)]
         _U64P = ctypes.POINTER(ctypes.c_uint64)
         L.kt_engine_parse_tsv.argtypes = [_VP, _VP, ctypes.c_uint64, _VP, _VP, ctypes.c_uint64, _U64P, _U32P]
         L.kt_engine_read_tsv.argtypes = [_VP, ctypes.c_char_p, _VP, _VP, ctypes.c_uint64, _U64P, _U32P]
@@ -439,6 +441,15 @@ class Engine:
         """The reference's tiled COO/CSR layout of a device entry list (kt_engine_tiled_coocsr)."""
         _check(lib().kt_engine_tiled_coocsr(self._h, d_src, d_dst, num_entries, num_nodes, tiles_per_dim,
                                             d_tile_src_ptr, d_src_out, d_dst_out))
+
+    def symmetrize(self, d_src: int, d_dst: int, num_entries: int, num_nodes: int, d_src_out: int, d_dst_out: int,
+                   capacity: int) -> int:
+        """Symmetric simple graph of a device entry list (kt_engine_symmetrize): directions merged,
+        duplicates and self loops dropped; returns the number of entries written (2 per edge)."""
+        out = ctypes.c_uint64(0)
+        _check(lib().kt_engine_symmetrize(self._h, d_src, d_dst, num_entries, num_nodes, d_src_out, d_dst_out,
+                                          capacity, ctypes.byref(out)))
+        return out.value
 
     def set_selector(self, selector: Optional["Selector"]) -> None:
         """Attach a learned selector (its schedule is used by every decomposition) or detach (None)."""
