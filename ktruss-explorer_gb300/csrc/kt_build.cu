@@ -142,12 +142,19 @@ __global__ void k_orient(const uint64_t* __restrict__ keys, uint64_t entries, un
     }
 }
 
+// fence[f] = o_col[32 f]: the first level of every search in an oriented row (fenced_lower_bound).
+__global__ void k_fences(const uint32_t* __restrict__ o_col, uint32_t m, uint32_t* __restrict__ fence) {
+    const uint32_t f = blockIdx.x * blockDim.x + threadIdx.x;
+    if ((uint64_t)f * 32 < m) fence[f] = o_col[(uint64_t)f * 32];
+}
+
 // Lower-rank entries (row r, column c < r) take the id of edge (c, r) from c's oriented row.
 // The oriented CSR must hold exactly m = entries / 2 edges; an input that is not symmetric can
 // leave rows that do not nest in [0, m): they are flagged, never searched.
 __global__ void k_in_eid(const uint64_t* __restrict__ keys, uint64_t entries, unsigned vb, uint32_t n, uint32_t m,
                          const uint32_t* __restrict__ o_ptr, const uint32_t* __restrict__ o_col,
-                         uint32_t* __restrict__ s_eid, uint32_t* __restrict__ ctrl) {
+                         const uint32_t* __restrict__ fence, uint32_t* __restrict__ s_eid,
+                         uint32_t* __restrict__ ctrl) {
     uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     uint32_t err = 0;
     if (p == 0 && o_ptr[n] != m) err = kErrAsymmetric;
@@ -159,7 +166,7 @@ __global__ void k_in_eid(const uint64_t* __restrict__ keys, uint64_t entries, un
             uint32_t idx = 0xffffffffu;
             if (lo <= hi && hi <= m) {
                 const uint32_t len = hi - lo;
-                idx = lower_bound_u32(o_col + lo, len, row);
+                idx = fenced_lower_bound(o_col, fence, lo, hi, row) - lo;
                 if (idx >= len || o_col[lo + idx] != row) idx = 0xffffffffu;
             }
             if (idx != 0xffffffffu) s_eid[p] = lo + idx;
@@ -470,9 +477,14 @@ int build_graph(kt_engine* e, const uint32_t* d_src, const uint32_t* d_dst, uint
         count_launch(e);
         if ((rc = check_launch(e, "k_orient"))) return rc;
     }
+    if (e->m) {
+        k_fences<<<grid_for((e->m + 31) / 32), kThreads, 0, st>>>(e->o_col, e->m, e->o_fence);
+        count_launch(e);
+        if ((rc = check_launch(e, "k_fences"))) return rc;
+    }
     if (entries) {
-        k_in_eid<<<grid_for(entries), kThreads, 0, st>>>(keys, entries, vb, n, e->m, e->o_ptr, e->o_col, e->s_eid,
-                                                         e->ctrl);
+        k_in_eid<<<grid_for(entries), kThreads, 0, st>>>(keys, entries, vb, n, e->m, e->o_ptr, e->o_col, e->o_fence,
+                                                         e->s_eid, e->ctrl);
         count_launch(e);
         if ((rc = check_launch(e, "k_in_eid"))) return rc;
         k_entry_eid<<<grid_for(entries), kThreads, 0, st>>>(e->sorted_entry, e->s_eid, entries, e->entry_eid);

@@ -74,6 +74,34 @@ __device__ __forceinline__ uint32_t lower_bound_u32(const uint32_t* __restrict__
     return lo;
 }
 
+// Lower bound of t in the sorted row a[lo, hi) of an array whose every 32nd element is copied to
+// fence[] (fence[f] = a[32 f]).  Rows longer than 32 entries are first searched in their fences,
+// which lie in a 32x smaller array, then in one block of at most 32 entries (one or two 128-byte
+// lines), so a search reads at most two lines of `a` instead of one per halving.
+__device__ __forceinline__ uint32_t fenced_lower_bound(const uint32_t* __restrict__ a,
+                                                       const uint32_t* __restrict__ fence, uint32_t lo,
+                                                       uint32_t hi, uint32_t t) {
+    if (hi - lo > 32) {
+        const uint32_t f0 = (lo + 31) >> 5, f1 = (hi - 1) >> 5;  // fences inside the row
+        uint32_t f = f0, n = f1 - f0 + 1;                         // first fence >= t
+        while (n > 0) {
+            const uint32_t half = n >> 1;
+            if (__ldg(fence + f + half) < t) {
+                f += half + 1;
+                n -= half + 1;
+            } else {
+                n = half;
+            }
+        }
+        // the answer lies in (32 (f-1), 32 f] (or [lo, 32 f0] when no fence is below t)
+        const uint32_t s = f == f0 ? lo : 32 * (f - 1) + 1;
+        const uint32_t e = 32 * f + 1 < hi ? 32 * f + 1 : hi;
+        lo = s;
+        hi = e;
+    }
+    return lo + lower_bound_u32(a + lo, hi - lo, t);
+}
+
 inline uint32_t ceil_div(uint64_t a, uint64_t b) { return (uint32_t)((a + b - 1) / b); }
 
 __device__ __forceinline__ uint32_t ld_acquire(const uint32_t* p) {

@@ -65,6 +65,7 @@ size_t carve(kt_engine* e, char* base, uint32_t n, uint64_t N, bool staging) {
     e->s_col = c.take<uint32_t>(N);
     e->s_eid = c.take<uint32_t>(N);
     e->o_col = c.take<uint32_t>(m);
+    e->o_fence = c.take<uint32_t>(m / 32 + 2);  // every 32nd oriented column
     e->e_src = c.take<uint32_t>(m);
     e->sup = c.take<uint32_t>(m + 4);  // read four at a time
     e->rnd = c.take<uint32_t>(m);

@@ -44,6 +44,7 @@ struct kt_engine {
     uint32_t* entry_eid = nullptr;     // edge id of each input entry (outputs are gathered by it)
     // Per edge (m); edge id = position in the oriented CSR.
     uint32_t* o_col = nullptr;    // higher-rank endpoint
+    uint32_t* o_fence = nullptr;  // o_fence[f] = o_col[32 f]: the first level of row searches
     uint32_t* e_src = nullptr;    // lower-rank endpoint
     uint32_t* sup = nullptr;      // support (alive triangles)
     uint32_t* rnd = nullptr;      // 0 while alive, else the peel round that removed it
