@@ -114,6 +114,8 @@ void remember(kt_engine* e, const kt_engine::LastCall& c) {
         l.truss != c.truss || l.k_max != c.k_max || l.k != c.k || l.keep != c.keep)
         drop_replay(e);
     e->last = c;
+    e->last.big_row = e->big_row;  // the build of the call being remembered set these
+    e->last.tiny_row = e->tiny_row;
 }
 
 void forget(kt_engine* e) {
@@ -249,6 +251,8 @@ int run_ktruss(kt_engine* e, const uint32_t* d_src, const uint32_t* d_dst, uint6
 // of the call itself): no host reads, so it can be captured into a CUDA graph.
 int replay_pipeline(kt_engine* e) {
     const kt_engine::LastCall& c = e->last;
+    e->big_row = c.big_row;  // other calls since may have built other graphs
+    e->tiny_row = c.tiny_row;
     int rc;
     if ((rc = kt::build_graph(e, c.src, c.dst, c.entries, c.n))) return rc;
     if (c.kind == 1)

@@ -109,6 +109,7 @@ struct kt_engine {
         uint32_t* k_max = nullptr;
         uint32_t k = 0;
         uint8_t* keep = nullptr;
+        uint32_t big_row = 0, tiny_row = 0;  // read back by the call's build; a trusted build does not
     } last;
     cudaGraphExec_t replay = nullptr;
     bool replay_direct = false;      // the pipeline could not be captured: replays launch it directly

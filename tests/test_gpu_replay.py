@@ -102,6 +102,29 @@ def test_replay_follows_the_last_call_and_schedule(torch):
     assert np.array_equal(o1.cpu().numpy().view(np.uint32), ref1["truss"])
 
 
+def test_replay_after_other_work_on_the_engine(torch):
+    """Features of another graph and a symmetrize call in between rebuild the workspace; the
+    replay still repeats the remembered call exactly."""
+    n1, src1, dst1, s1, t1 = _device_graph(torch, GRAPHS[1][1])
+    n2, src2, dst2, s2, t2 = _device_graph(torch, lambda: kt.gen_rmat(12, 16, 0.57, 0.19, 0.19, 37))
+    ref1 = oracle.decompose(n1, src1, dst1, method="peel")
+    eng = kt.Engine(0)
+    o1 = torch.empty(len(src1), dtype=torch.int32, device="cuda")
+    k = torch.zeros(1, dtype=torch.int32, device="cuda")
+    so = torch.empty(2 * len(src2), dtype=torch.int32, device="cuda")
+    do = torch.empty(2 * len(src2), dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    eng.decompose(s1.data_ptr(), t1.data_ptr(), len(src1), n1, o1.data_ptr(), k.data_ptr())
+    eng.replay()
+    eng.features(s2.data_ptr(), t2.data_ptr(), len(src2), n2)
+    eng.symmetrize(s2.data_ptr(), t2.data_ptr(), len(src2), n2, so.data_ptr(), do.data_ptr(), 2 * len(src2))
+    o1.fill_(-1)
+    torch.cuda.synchronize()
+    eng.replay()
+    assert int(k.item()) == ref1["k_max"]
+    assert np.array_equal(o1.cpu().numpy().view(np.uint32), ref1["truss"])
+
+
 def test_replay_needs_a_successful_call(torch):
     eng = kt.Engine(0)
     with pytest.raises(kt.KtrussError) as ei:
