@@ -59,12 +59,23 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
     return m;
 }
 
+// Read-only load: the non-coherent cache path on the device, a plain load in host builds of the
+// search helpers below (their unit test runs them on the CPU).
+__host__ __device__ __forceinline__ uint32_t ld_ro(const uint32_t* p) {
+#ifdef __CUDA_ARCH__
+    return __ldg(p);
+#else
+    return *p;
+#endif
+}
+
 // Index of the first element >= x in sorted a[0, n) (lower bound).
-__device__ __forceinline__ uint32_t lower_bound_u32(const uint32_t* __restrict__ a, uint32_t n, uint32_t x) {
+__host__ __device__ __forceinline__ uint32_t lower_bound_u32(const uint32_t* __restrict__ a, uint32_t n,
+                                                             uint32_t x) {
     uint32_t lo = 0;
     while (n > 0) {
         uint32_t half = n >> 1;
-        if (__ldg(a + lo + half) < x) {
+        if (ld_ro(a + lo + half) < x) {
             lo += half + 1;
             n -= half + 1;
         } else {
@@ -78,15 +89,15 @@ __device__ __forceinline__ uint32_t lower_bound_u32(const uint32_t* __restrict__
 // fence[] (fence[f] = a[32 f]).  Rows longer than 32 entries are first searched in their fences,
 // which lie in a 32x smaller array, then in one block of at most 32 entries (one or two 128-byte
 // lines), so a search reads at most two lines of `a` instead of one per halving.
-__device__ __forceinline__ uint32_t fenced_lower_bound(const uint32_t* __restrict__ a,
-                                                       const uint32_t* __restrict__ fence, uint32_t lo,
-                                                       uint32_t hi, uint32_t t) {
+__host__ __device__ __forceinline__ uint32_t fenced_lower_bound(const uint32_t* __restrict__ a,
+                                                                const uint32_t* __restrict__ fence, uint32_t lo,
+                                                                uint32_t hi, uint32_t t) {
     if (hi - lo > 32) {
         const uint32_t f0 = (lo + 31) >> 5, f1 = (hi - 1) >> 5;  // fences inside the row
         uint32_t f = f0, n = f1 - f0 + 1;                         // first fence >= t
         while (n > 0) {
             const uint32_t half = n >> 1;
-            if (__ldg(fence + f + half) < t) {
+            if (ld_ro(fence + f + half) < t) {
                 f += half + 1;
                 n -= half + 1;
             } else {
