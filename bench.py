@@ -632,6 +632,10 @@ def run_ours(args, world, rank, local):
     ev3.record(stream)
     torch.cuda.synchronize()
     replay_ms = ev2.elapsed_time(ev3) / args.steps
+    try:
+        replay_mode = eng.replay_mode()
+    except Exception as exc:  # informational only
+        replay_mode = f"unknown ({exc})"
     if not torch.equal(d_out, ref_out):
         raise RuntimeError("replayed decomposition differs")
 
@@ -681,7 +685,7 @@ def run_ours(args, world, rank, local):
                                     "peel": statistics.mean(peel_ms)},
                        "peel_phase_ms": st.as_dict()["peel_phase_ms"], "compactions": st.compactions,
                        "walk_entries": st.walk_entries,
-                       "replay": {"ms_per_step": replay_ms,
+                       "replay": {"ms_per_step": replay_ms, "mode": replay_mode,
                                   "how": "kt_engine_replay: the same steps through a CUDA graph of the device "
                                          "pipeline (repeat runs on unchanged input, no host-side input checks)"},
                        "schedule": sched},

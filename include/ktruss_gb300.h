@@ -234,6 +234,9 @@ int kt_engine_ktruss(kt_engine* engine, const uint32_t* d_src, const uint32_t* d
  * A different call, a new schedule or selector, or a larger reservation drops the graph.
  * Statistics afterwards: everything but the per-phase times (0); last_ms is the replay's. */
 int kt_engine_replay(kt_engine* engine, int sync);
+/* How the next replay runs: 0 nothing to replay yet or not captured yet, 1 one launch of the
+ * captured CUDA graph, 2 direct launches (the capture was refused). */
+int kt_engine_replay_mode(const kt_engine* engine);
 /* Batched decomposition (no counterpart in the reference): num_graphs graphs in one call, given
  * as one COO over disjoint vertex ranges — graph g owns vertices [d_vertex_offsets[g],
  * d_vertex_offsets[g+1]), num_graphs+1 offsets ending at num_nodes, and every entry stays inside

@@ -439,6 +439,8 @@ int kt_engine_replay(kt_engine* e, int sync) {
     return replay(e, sync);
 }
 
+int kt_engine_replay_mode(const kt_engine* e) { return !e ? 0 : e->replay ? 1 : e->replay_direct ? 2 : 0; }
+
 kt_schedule kt_schedule_default(void) { return kt_schedule{8, 32, 85, 50, 0}; }
 
 int kt_engine_set_schedule(kt_engine* e, const kt_schedule* s) {

@@ -132,6 +132,7 @@ def lib() -> ctypes.CDLL:
         L.kt_engine_ktruss.argtypes = [_VP, _VP, _VP, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32, _VP,
                                        ctypes.c_int]
         L.kt_engine_replay.argtypes = [_VP, ctypes.c_int]
+        L.kt_engine_replay_mode.argtypes = [_VP]
         L.kt_engine_stats.argtypes = [_VP, ctypes.POINTER(Stats)]
         L.kt_last_stats.argtypes = [ctypes.POINTER(Stats)]
         L.kt_engine_selftest_barrier_timeout.argtypes = [_VP, ctypes.c_uint64]
@@ -392,6 +393,10 @@ class Engine:
         """Repeats the last decompose/ktruss call on the same (unchanged) device buffers through
         a CUDA graph of its device pipeline, captured at the first replay."""
         _check(lib().kt_engine_replay(self._h, int(sync)))
+
+    def replay_mode(self) -> str:
+        """How the next replay runs: "cuda graph", "direct launches" or "none" (not captured yet)."""
+        return {1: "cuda graph", 2: "direct launches"}.get(lib().kt_engine_replay_mode(self._h), "none")
 
     def set_schedule(self, support_group: int = 8, chunk_width: int = 32, compact_percent: int = 85,
                      recount_percent: int = 50, peel_blocks: int = 0) -> None:

@@ -54,6 +54,7 @@ def test_replayed_decomposition_is_identical(name, make, torch):
         assert st.last_ms > 0 and st.build_ms == 0
         assert st.kernel_launches > launches  # the graph's kernels are counted
         launches = st.kernel_launches
+    assert eng.replay_mode() in ("cuda graph", "direct launches")
 
 
 def test_replayed_single_k_truss(torch):
