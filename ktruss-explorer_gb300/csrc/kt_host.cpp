@@ -9,6 +9,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <getopt.h>
+#include <thread>
 #include <vector>
 
 namespace kt {
@@ -309,14 +310,56 @@ int kt_read_tsv(const char* path, kt_coo* out) {
     return KT_OK;
 }
 
+// Decimal digits of x at p; returns the end.
+static char* put_u64(char* p, uint64_t x) {
+    char tmp[20];
+    int n = 0;
+    do {
+        tmp[n++] = (char)('0' + x % 10);
+        x /= 10;
+    } while (x);
+    while (n) *p++ = tmp[--n];
+    return p;
+}
+
+// Lines "dst+1 \t src+1 \t third" of entries [e0, e1) into out (at most 33 bytes a line).
+static size_t format_entries(const kt_coo* g, const uint32_t* third, uint64_t e0, uint64_t e1, char* out) {
+    char* p = out;
+    for (uint64_t e = e0; e < e1; ++e) {
+        p = put_u64(p, (uint64_t)g->dst_idx[e] + 1);
+        *p++ = '\t';
+        p = put_u64(p, (uint64_t)g->src_idx[e] + 1);
+        *p++ = '\t';
+        p = put_u64(p, third ? third[e] : 1u);
+        *p++ = '\n';
+    }
+    return (size_t)(p - out);
+}
+
+// The reference writes one fprintf per entry (graph.cu:96-104); here batches of entries are
+// formatted by all host threads, each into its own buffer, and written in order.
 static int write_entries(const kt_coo* g, const uint32_t* third, const char* path) {
-    FILE* fp = fopen(path, "w");
+    FILE* fp = fopen(path, "wb");
     if (!fp) return fail(KT_ERR_IO, "cannot open %s for writing: %s", path, strerror(errno));
-    std::vector<char> buf(1 << 20);
-    setvbuf(fp, buf.data(), _IOFBF, buf.size());
-    for (uint32_t e = 0; e < g->num_edges; ++e)
-        fprintf(fp, "%u\t%u\t%u\n", g->dst_idx[e] + 1, g->src_idx[e] + 1, third ? third[e] : 1u);
-    if (fclose(fp) != 0) return fail(KT_ERR_IO, "write to %s failed", path);
+    const uint64_t m = g->num_edges;
+    const unsigned hw = std::thread::hardware_concurrency();
+    const uint64_t threads = std::max<uint64_t>(1, std::min<uint64_t>(hw ? hw : 1, 32));
+    const uint64_t per = 1u << 18;  // entries per thread and batch
+    std::vector<std::vector<char>> bufs(threads, std::vector<char>(per * 33));
+    std::vector<size_t> used(threads);
+    bool failed = false;
+    for (uint64_t b0 = 0; b0 < m && !failed; b0 += per * threads) {
+        std::vector<std::thread> pool;
+        for (uint64_t t = 0; t < threads; ++t) {
+            const uint64_t e0 = std::min(m, b0 + t * per), e1 = std::min(m, e0 + per);
+            used[t] = 0;
+            if (e0 < e1) pool.emplace_back([&, t, e0, e1] { used[t] = format_entries(g, third, e0, e1, bufs[t].data()); });
+        }
+        for (auto& th : pool) th.join();
+        for (uint64_t t = 0; t < threads && !failed; ++t)
+            if (used[t] && fwrite(bufs[t].data(), 1, used[t], fp) != used[t]) failed = true;
+    }
+    if (fclose(fp) != 0 || failed) return fail(KT_ERR_IO, "write to %s failed", path);
     return KT_OK;
 }
 

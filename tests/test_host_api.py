@@ -71,6 +71,27 @@ def test_tsv_roundtrip(tmp_path):
     assert third == list(np.concatenate([t, t]))
 
 
+def test_tsv_writer_bytes(tmp_path):
+    """Parallel formatting gives the same bytes as one formatted line per entry, across batch
+    boundaries (2.5 M entries) and at the largest ids and third-column values."""
+    rng = np.random.default_rng(12)
+    m = 2_500_000
+    src = rng.integers(0, 2**32 - 1, m, dtype=np.uint64).astype(np.uint32)
+    dst = rng.integers(0, 2**32 - 1, m, dtype=np.uint64).astype(np.uint32)
+    third = rng.integers(0, 2**32, m, dtype=np.uint64).astype(np.uint32)
+    src[:3] = [0, 2**32 - 2, 7]
+    third[:3] = [0, 2**32 - 1, 9]
+    g = kt.COOGraph(2**32 - 1, src, dst)
+    p = tmp_path / "w.tsv"
+    kt.write_truss_to_file(g, third, str(p))
+    d1, s1, t1 = dst.astype(np.int64) + 1, src.astype(np.int64) + 1, third.astype(np.int64)
+    want = "".join(f"{a}\t{b}\t{c}\n" for a, b, c in zip(d1.tolist(), s1.tolist(), t1.tolist()))
+    assert p.read_bytes() == want.encode()
+    q = tmp_path / "g.tsv"
+    kt.write_coo_graph_to_file(kt.COOGraph(2**32 - 1, src[:1000], dst[:1000]), str(q))
+    assert q.read_text() == "".join(f"{a}\t{b}\t1\n" for a, b in zip(d1[:1000].tolist(), s1[:1000].tolist()))
+
+
 def test_tsv_errors(tmp_path):
     with pytest.raises(kt.KtrussError) as ei:
         kt.create_coo_from_file(str(tmp_path / "missing.tsv"))
