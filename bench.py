@@ -1,26 +1,34 @@
-"""Benchmark: full k-truss decomposition of R-MAT scale 20 (edge factor 16) on one GB300.
+"""Benchmark: k-truss on R-MAT scale 20 (edge factor 16, seed 1) on one GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload rmat20]
 
-One step = one decomposition (device CSR build from the COO entries, support count, peeling,
-per-entry truss numbers) of the whole graph.  Prints one JSON line.
+Prints one JSON line.  Both arms print the same `metric` ("k-truss edges/s") and `config` (the
+graph); `work` says what one step computes.
 
+ours (one step = one full truss decomposition: device CSR build from the COO entries, support
+count, peeling of every level, per-entry truss numbers)
   value       edges/s = m / t_step with the COO input already in HBM (engine API, device buffers)
-  e2e         edges/s through the host-buffer C ABI call kt_decompose: the pinned input entries
+  e2e         the same through the host-buffer C ABI call kt_decompose: the pinned input entries
               are copied host->device and the per-entry truss numbers device->host every step
   roofline    the dominant kernel, the persistent peel (one launch per decomposition): algorithmic
               bytes per launch = the bytes of the reference's full-recount schedule for the
               passes that launch covers, sum over passes p of 4(n+1) + 12 E+_p (row pointers,
-              column array, support written and read once per pass), over the kernel's CUDA-event
-              time, against the measured HBM copy bandwidth; the support-count kernel's figure
-              (4(n+1) + 12m per launch) is reported beside it
-  cpu_baseline  the reference algorithm (oracle port of its CPU path: chained count-and-prune
-              passes over k) timed on a bounded sample of passes on one host core, scaled to the
-              whole decomposition by the workload's exact pass volume (sum of alive edges over
-              all passes of the reference schedule)
+              column array, support written and read once per pass), with the pass counts taken
+              from the oracle fixture (tests/golden/rmat20_seed1.json), over the kernel's
+              CUDA-event time, against the measured HBM copy bandwidth; the support-count
+              kernel's figure (4(n+1) + 12m per launch) is reported beside it
+  single_k3   the reference's own unit of work on the same graph - one single-k run at k = 3 -
+              through kt_engine_ktruss, for a like-for-like comparison with the reference arm
+  cpu_baseline  that unit on the host cores: the oracle port of the reference loop
+              (kernel_hdc.cu:107-201, count and mark sweeps split over all host threads), complete
+              runs timed like the reference's k-truss timer
 
---impl reference times only that CPU port (building the reference's own executable needs its
-sources, which this package does not ship) and prints the same line with impl "reference".
+reference (--impl reference; one step = one complete single-k run at k = 3 on the whole graph,
+the span the reference's k-truss timer measures, kernel_hdc.cu:213-229): the oracle port of the
+reference's CPU loop on all host threads, after W warm-up runs, as the reference's -w/-x repeat
+runs.  The graph comes from the oracle's own generator; the product library is not loaded.  A
+complete CPU decomposition of this graph takes hours (a stratified estimate is made by
+--decomposition-estimate and recorded separately, never as `value`).
 Under torchrun, each rank decomposes its own replica (the single-graph path does not shard).
 """
 from __future__ import annotations
@@ -63,11 +71,31 @@ BATCHES = {
 # (other seed), never on the graphs that are measured.
 TUNE_SAMPLE = dict(num_graphs=256, seed=1001)
 
-# Exact pass volume of the reference schedule for each workload (number of count-and-prune
-# passes of the chained single-k runs and the sum of their alive oriented edges).  The engine
-# recomputes both every run and bench.py checks them; the reference arm needs them to scale its
-# bounded sample to the whole decomposition.
-PASS_VOLUME = {"rmat20": {"plain_passes": 2470, "plain_alive_sum": 7079259210}}
+# Oracle fixtures of the single-graph workloads (tests/golden/make_headline_fixture.py): truss-number
+# hash and histogram, k_max, and the pass statistics of the reference schedule (per level k the
+# count-and-prune passes and their alive oriented edges).  The roofline's algorithmic bytes come
+# from these, and every run is checked against them.
+FIXTURES = {"rmat20": os.path.join(ROOT, "tests", "golden", "rmat20_seed1.json")}
+
+
+def fixture(name):
+    path = FIXTURES.get(name)
+    if not path or not os.path.exists(path):
+        return None
+    with open(path) as f:
+        return json.load(f)
+
+
+def workload_config(name, n, m):
+    """The `config` both arms print for a single-graph workload (the graph, not the method)."""
+    w = WORKLOADS[name]
+    desc = (f"{name}: R-MAT scale {w['scale']}, edge factor {w['ef']}, (a,b,c,d) = ({w['a']},{w['b']},{w['c']},"
+            f"{round(1 - w['a'] - w['b'] - w['c'], 2)}), seed {w['seed']}, symmetrized, deduplicated, self loops "
+            "removed")
+    if "cliques" in w:
+        desc += f", {w['cliques'][0]} planted cliques of {w['cliques'][1]}-{w['cliques'][2]} vertices"
+    return {"workload": desc, "n": n, "m": m, "l2": "input entries 2x4x2m bytes > L2 (129 MB)"}
+
 
 FALLBACK_HBM_GBS = 6800.0
 
@@ -81,17 +109,47 @@ def peaks():
         return FALLBACK_HBM_GBS, "fallback"
 
 
-def make_graph(name):
-    import ktruss_gb300 as kt
-
+def make_graph(name, with_oracle=False):
+    """(n, m, src, dst) of a single-graph workload; with_oracle: made by the oracle's generator
+    (the same graph, without loading the product library)."""
     w = WORKLOADS[name]
-    n, u, v = kt.gen_rmat(w["scale"], w["ef"], w["a"], w["b"], w["c"], w["seed"])
-    if "cliques" in w:
-        count, lo, hi = w["cliques"]
-        n, u, v = kt.plant_cliques(n, u, v, count, lo, hi, w["seed"] + 7)
+    if with_oracle:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle
+
+        if "cliques" in w:
+            raise ValueError(f"{name}: the oracle has no clique planter")
+        n, u, v = oracle.gen_rmat(w["scale"], w["ef"], w["a"], w["b"], w["c"], w["seed"])
+    else:
+        import ktruss_gb300 as kt
+
+        n, u, v = kt.gen_rmat(w["scale"], w["ef"], w["a"], w["b"], w["c"], w["seed"])
+        if "cliques" in w:
+            count, lo, hi = w["cliques"]
+            n, u, v = kt.plant_cliques(n, u, v, count, lo, hi, w["seed"] + 7)
     src = np.concatenate([u, v]).astype(np.uint32)
     dst = np.concatenate([v, u]).astype(np.uint32)
     return n, len(u), src, dst
+
+
+def load_er4096():
+    """The Erdos-Renyi G(4096, 16/4095) graph of the golden fixtures (the plain method's small
+    configuration): (n, src, dst, truss per edge, k_max)."""
+    import gzip
+
+    with open(os.path.join(ROOT, "tests", "golden", "manifest.json")) as f:
+        man = json.load(f)["graphs"]["er4096"]
+    with gzip.open(os.path.join(ROOT, "tests", "golden", "er4096.tsv.gz"), "rt") as f:
+        data = np.loadtxt(f, dtype=np.int64, ndmin=2)
+    u, v, t = data[:, 0].astype(np.uint32), data[:, 1].astype(np.uint32), data[:, 2].astype(np.uint32)
+    return man["num_nodes"], np.concatenate([u, v]), np.concatenate([v, u]), t, man["k_max"]
+
+
+def host_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:
+        return os.cpu_count() or 1
 
 
 class ClockSampler:
@@ -180,57 +238,118 @@ def replica_throughput(m: int, world: int, ms: float) -> float:
     return m * world / (ms * 1e-3)
 
 
-def cpu_sample(n, src, dst, budget_s, pass_volume):
-    """Times the oracle port of the reference's CPU algorithm on a bounded prefix of its passes."""
+def oracle_module():
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
 
-    s = oracle.chain_sample(n, src, dst, budget_s)
-    rate = s["alive_sum"] / s["seconds"]  # alive oriented edges processed per second
-    return s, rate
+    return oracle
+
+
+def k3_runs_cpu(n, src, dst, warmup, runs, threads):
+    """The reference's timed unit on the host cores: single-k runs at k = 3 on the whole graph by the
+    oracle port of its loop (count and mark sweeps split over `threads` threads), `warmup` untimed
+    runs first.  Returns (seconds per timed run, passes per run, edges kept by the last run)."""
+    oracle = oracle_module()
+    os_, _, secs, passes = oracle.ktruss_runs(n, src, dst, 3, warmup + runs, threads)
+    return secs[warmup:], passes[warmup:], len(os_) // 2
+
+
+def er4096_chain_cpu():
+    """The plain method's small configuration (Erdos-Renyi G(4096, 16/4095)) decomposed completely by
+    the reference algorithm (chained single-k runs, one host thread), checked against its fixture."""
+    oracle = oracle_module()
+    n, src, dst, t, k_max = load_er4096()
+    t0 = time.perf_counter()
+    r = oracle.decompose(n, src, dst, method="chain", threads=1)
+    secs = time.perf_counter() - t0
+    if r["k_max"] != k_max or not np.array_equal(r["truss"][: len(t)], t):
+        raise RuntimeError("oracle chain differs from the er4096 fixture")
+    m = len(t)
+    return {"ms": secs * 1e3, "edges_per_s": m / secs, "m": m, "k_max": k_max, "passes": r["plain_passes"],
+            "how": "complete decomposition, chained single-k runs k = 3, 4, ... (reference algorithm), one host "
+                   "thread"}
+
+
+def decomposition_estimate(n, m, src, dst, threads, strata):
+    """Stratified estimate of the reference's complete chained decomposition on the host cores: the
+    chain's levels (k = 3 .. k_max+1, each a single-k run on the (k-1)-truss) are cut into `strata`
+    groups of equal alive-edge volume; from each group the level at its volume midpoint runs once,
+    completely, on its chain input; a group's time is the run's time scaled by the group's volume
+    over the level's.  An extrapolation, reported apart from `value`."""
+    oracle = oracle_module()
+    t0 = time.perf_counter()
+    r = oracle.decompose(n, src, dst, levels=True, threads=threads)
+    truss = r["truss"][:m]
+    u, v = src[:m], dst[:m]
+    lp, la = r["level_passes"], r["level_alive"]
+    ks = [k for k in range(len(lp)) if lp[k]]
+    vol = np.array([float(la[k]) for k in ks])
+    total = vol.sum()
+    cum = np.cumsum(vol)
+    groups, start = [], 0
+    for gi in range(strata):
+        end = int(np.searchsorted(cum, total * (gi + 1) / strata - 1e-9)) + 1
+        end = max(end, start + 1)
+        if start >= len(ks):
+            break
+        groups.append((start, min(end, len(ks))))
+        start = min(end, len(ks))
+    rows, est = [], 0.0
+    for a, b in groups:
+        gvol = vol[a:b].sum()
+        mid = cum[a] - vol[a] + gvol / 2  # volume midpoint of the group
+        i = min(int(np.searchsorted(cum, mid)), b - 1)
+        k = ks[i]
+        sel = truss >= k - 1 if k > 3 else np.ones(m, bool)
+        s_in = np.concatenate([u[sel], v[sel]])
+        d_in = np.concatenate([v[sel], u[sel]])
+        _, _, secs, passes = oracle.ktruss_runs(n, s_in, d_in, k, 1, threads)
+        if int(passes[0]) != int(lp[k]):
+            raise RuntimeError(f"level {k}: {int(passes[0])} passes, the peel says {int(lp[k])}")
+        est += float(secs[0]) * gvol / vol[i]
+        rows.append({"k": int(k), "levels": [int(ks[a]), int(ks[b - 1])], "input_edges": int(sel.sum()),
+                     "passes": int(passes[0]), "seconds": float(secs[0]), "group_volume_share": gvol / total})
+    return {"chain_seconds_extrapolated": est, "threads": threads, "strata": rows,
+            "levels_total": len(ks), "timed_volume_share": sum(float(la[x["k"]]) for x in rows) / total,
+            "edges_per_s_extrapolated": m / est, "setup_s": time.perf_counter() - t0,
+            "how": "stratified by alive-edge volume; one complete single-k run per stratum on its chain input "
+                   "(the (k-1)-truss from the oracle peel), scaled by the stratum's volume"}
 
 
 def run_reference(args, world, rank):
     if rank != 0:
         return
-    if args.workload not in WORKLOADS:
-        print(json.dumps({"impl": "reference", "unavailable": "the reference CPU arm is timed on the single-graph "
-                                                              "workloads (the reference has no batch or selector)"}))
+    w = WORKLOADS.get(args.workload)
+    if w is None or "cliques" in w:
+        print(json.dumps({"impl": "reference", "unavailable": "the reference CPU arm runs the single-graph R-MAT "
+                                                              "workloads without planted cliques (the reference has "
+                                                              "no batch or selector; the oracle plants no cliques)"}))
         return
-    n, m, src, dst = make_graph(args.workload)
-    vol = PASS_VOLUME.get(args.workload)
-    # untimed warm-up on a small graph (the sample's first pass alone is the full-graph count)
-    nw, mw, sw, dw = make_graph("rmat16")
-    for _ in range(args.warmup):
-        cpu_sample(nw, sw, dw, 0.0, None)
-    budget = max(1.0, 60.0 / max(1, args.steps))
-    rates, samples = [], []
+    n, m, src, dst = make_graph(args.workload, with_oracle=True)
+    fx = fixture(args.workload)
+    threads = host_threads()
     t0 = time.time()
-    for _ in range(args.steps):
-        s, rate = cpu_sample(n, src, dst, budget, vol)
-        rates.append(rate)
-        samples.append(s)
+    secs, passes, kept = k3_runs_cpu(n, src, dst, args.warmup, args.steps, threads)
     wall = time.time() - t0
-    rate = statistics.median(rates)
-    if vol:
-        t_full = vol["plain_alive_sum"] / rate
-        value = m / t_full
-        unit = "edges/s"
-        desc = (f"the start of the reference's chained decomposition: {samples[0]['passes']} complete of "
-                f"{vol['plain_passes']} count-and-prune passes plus the edges a cut pass had counted "
-                f"({samples[0]['alive_sum']} of {vol['plain_alive_sum']} alive-edge visits, graph set-up "
-                f"included), {samples[0]['seconds']:.1f} s per step; scaled by alive-edge volume")
-    else:
-        value, unit, t_full = rate, "alive-edge-visits/s", None
-        desc = "first passes of the chained decomposition (pass volume unknown: not scaled)"
-    line = {"metric": "k-truss decomposition edges/s", "value": value, "unit": unit, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": (t_full * 1e3) if t_full else None,
+    if fx and kept != fx["chained_checks"][0]["truss_edges"]:
+        raise RuntimeError(f"k = 3 kept {kept} edges, the fixture says {fx['chained_checks'][0]['truss_edges']}")
+    ms = float(np.mean(secs)) * 1e3
+    value = m / (ms * 1e-3)
+    sample = (f"{args.steps} complete single-k runs at k = 3 on the whole graph (after {args.warmup} warm-up "
+              f"runs): the oracle port of the reference's count-and-prune loop (kernel_hdc.cu:107-201, "
+              f"{int(passes[0])} pass, count and mark sweeps split over {threads} host threads), each timed alone "
+              "like the reference's k-truss timer (kernel_hdc.cu:213-229); relabel and CSR build once, untimed")
+    line = {"metric": "k-truss edges/s", "value": value, "unit": "edges/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-            "impl": "reference",
-            "config": {"workload": f"{args.workload} full truss decomposition", "m": m, "n": n},
-            "cpu_baseline": {"value": value, "unit": unit, "cores": 1, "kind": "port", "sample": desc},
-            "e2e": {"value": value, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "wall_s": wall}
+            "impl": "reference", "config": workload_config(args.workload, n, m),
+            "work": "one complete single-k run at k = 3 on the whole graph (the reference's timed unit)",
+            "cpu_baseline": {"value": value, "unit": "edges/s", "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": "edges/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "run_ms": [float(x) * 1e3 for x in secs], "kept_edges": kept,
+            "er4096_full_decomposition": er4096_chain_cpu(), "wall_s": wall}
+    if args.decomposition_estimate:
+        line["decomposition_estimate"] = decomposition_estimate(n, m, src, dst, threads, args.decomposition_estimate)
     print(json.dumps(line), flush=True)
 
 
@@ -601,16 +720,10 @@ def run_ours(args, world, rank, local):
         td.barrier()
     torch.cuda.synchronize()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    support_ms, build_ms, peel_ms, peel_kernel_ms = [], [], [], []
     with ClockSampler(local) as clk:
         ev0.record(stream)
         for _ in range(args.steps):
             step()
-            s = eng.stats()
-            support_ms.append(s.support_ms)
-            build_ms.append(s.build_ms)
-            peel_ms.append(s.peel_ms)
-            peel_kernel_ms.append(s.peel_kernel_ms)
         ev1.record(stream)
         torch.cuda.synchronize()
     ms = ev0.elapsed_time(ev1) / args.steps
@@ -619,6 +732,33 @@ def run_ours(args, world, rank, local):
     if dist:
         ms = max_over_ranks(ms, td, "cuda")
     k_max = int(d_k.item())
+    truss = d_out.cpu().numpy().view(np.uint32)
+
+    # phase breakdown: the same step again, one at a time (stats read after each)
+    phases = {"build": [], "support": [], "peel": [], "peel_kernel": []}
+    for _ in range(min(args.steps, 5)):
+        step()
+        s_ = eng.stats()
+        for key, val in (("build", s_.build_ms), ("support", s_.support_ms), ("peel", s_.peel_ms),
+                         ("peel_kernel", s_.peel_kernel_ms)):
+            phases[key].append(val)
+    st = eng.stats()
+    pm = {k_: statistics.mean(v_) for k_, v_ in phases.items()}
+
+    # parity with the oracle fixture of this graph (hash of the per-edge truss numbers, k_max, and
+    # the reference schedule's pass statistics)
+    fx = fixture(args.workload)
+    parity = None
+    if fx:
+        import hashlib
+
+        got = hashlib.sha256(np.ascontiguousarray(truss[:m]).astype("<u4").tobytes()).hexdigest()
+        if got != fx["truss_sha256"] or k_max != fx["k_max"] or not np.array_equal(truss[:m], truss[m:]):
+            raise RuntimeError("decomposition differs from the oracle fixture")
+        if st.plain_passes != fx["plain_passes"] or st.plain_alive_sum != fx["plain_alive_sum"]:
+            raise RuntimeError(f"pass statistics {st.plain_passes}/{st.plain_alive_sum} differ from the fixture")
+        parity = (f"per-edge truss numbers equal the oracle fixture {os.path.relpath(FIXTURES[args.workload], ROOT)} "
+                  f"(sha256 {got[:16]}...), k_max {k_max}, {fx['plain_passes']} reference passes")
 
     # the same steps as repeat runs on unchanged input: the CUDA graph of the whole device
     # pipeline (kt_engine_replay), captured at the first replay
@@ -639,6 +779,41 @@ def run_ours(args, world, rank, local):
     if not torch.equal(d_out, ref_out):
         raise RuntimeError("replayed decomposition differs")
 
+    # the reference's own unit on the same graph: single-k runs at k = 3 (kt_engine_ktruss)
+    d_keep = torch.empty(N, dtype=torch.uint8, device="cuda")
+    for _ in range(2):
+        eng.ktruss(d_src.data_ptr(), d_dst.data_ptr(), N, n, 3, d_keep.data_ptr(), sync=False)
+    torch.cuda.synchronize()
+    ev4, ev5 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev4.record(stream)
+    for _ in range(args.steps):
+        eng.ktruss(d_src.data_ptr(), d_dst.data_ptr(), N, n, 3, d_keep.data_ptr(), sync=False)
+    ev5.record(stream)
+    torch.cuda.synchronize()
+    k3_ms = ev4.elapsed_time(ev5) / args.steps
+    k3_kept = int(d_keep.sum().item()) // 2
+    if fx and k3_kept != fx["chained_checks"][0]["truss_edges"]:
+        raise RuntimeError("k = 3 truss differs from the fixture")
+
+    # the plain method's small configuration (Erdos-Renyi G(4096, 16/4095)), decomposed completely
+    en, es, ed, et, ek = load_er4096()
+    d_es = torch.from_numpy(es.view(np.int32)).cuda()
+    d_ed = torch.from_numpy(ed.view(np.int32)).cuda()
+    d_eo = torch.empty(len(es), dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    for _ in range(3):
+        eng.decompose(d_es.data_ptr(), d_ed.data_ptr(), len(es), en, d_eo.data_ptr(), d_k.data_ptr(), sync=False)
+    torch.cuda.synchronize()
+    ev6, ev7 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev6.record(stream)
+    for _ in range(args.steps):
+        eng.decompose(d_es.data_ptr(), d_ed.data_ptr(), len(es), en, d_eo.data_ptr(), d_k.data_ptr(), sync=False)
+    ev7.record(stream)
+    torch.cuda.synchronize()
+    er_ms = ev6.elapsed_time(ev7) / args.steps
+    if int(d_k.item()) != ek or not np.array_equal(d_eo.cpu().numpy().view(np.uint32)[: len(et)], et):
+        raise RuntimeError("er4096 decomposition differs from its fixture")
+
     # end to end through the host-buffer C ABI (pinned host memory)
     h_src = torch.from_numpy(src.view(np.int32)).pin_memory()
     h_dst = torch.from_numpy(dst.view(np.int32)).pin_memory()
@@ -656,7 +831,7 @@ def run_ours(args, world, rank, local):
     if dist:
         e2e_s = max_over_ranks(e2e_s, td, "cuda")
     assert k2 == k_max
-    if not np.array_equal(out_np, d_out.cpu().numpy().view(np.uint32)):
+    if not np.array_equal(out_np, truss):
         raise RuntimeError("host-buffer and device-buffer decompositions differ")
 
     hbm, hbm_kind = peaks()
@@ -666,58 +841,61 @@ def run_ours(args, world, rank, local):
             traffic = json.load(f).get(args.workload, {})
     except Exception:
         pass
-    sup_ms = statistics.mean(support_ms)
+    sup_ms = pm["support"]
     sup_bytes = 4 * (n + 1) + 12 * m
     sup_gbs = sup_bytes / (sup_ms * 1e-3) / 1e9
-    pk_ms = statistics.mean(peel_kernel_ms)
-    plain_bytes = 4 * (n + 1) * st.plain_passes + 12 * st.plain_alive_sum
+    pk_ms = pm["peel_kernel"]
+    passes = fx["plain_passes"] if fx else st.plain_passes
+    alive_sum = fx["plain_alive_sum"] if fx else st.plain_alive_sum
+    plain_bytes = 4 * (n + 1) * passes + 12 * alive_sum
     pk_gbs = plain_bytes / (pk_ms * 1e-3) / 1e9
-    vol = PASS_VOLUME.get(args.workload)
-    if vol and (vol["plain_passes"] != st.plain_passes or vol["plain_alive_sum"] != st.plain_alive_sum):
-        raise RuntimeError(f"pass volume changed: {st.plain_passes}/{st.plain_alive_sum} vs {vol}")
-    line = {"metric": "k-truss decomposition edges/s", "value": replica_throughput(m, world, ms), "unit": "edges/s",
+    traffic_note = traffic.get("source")
+    line = {"metric": "k-truss edges/s", "value": replica_throughput(m, world, ms), "unit": "edges/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-            "config": {"workload": f"{args.workload} full truss decomposition", "n": n, "m": m, "k_max": k_max,
-                       "triangles": st.triangles, "peel_rounds": st.num_rounds, "peel_levels": st.num_levels,
-                       "parallelism": f"replicas{world}", "l2": "input entries 2x4x2m bytes > L2 (129 MB)",
-                       "phase_ms": {"build": statistics.mean(build_ms), "support": sup_ms,
-                                    "peel": statistics.mean(peel_ms)},
+            "config": workload_config(args.workload, n, m),
+            "work": "one full truss decomposition (every k): device CSR build, support count, peel, per-entry "
+                    "truss numbers",
+            "detail": {"k_max": k_max, "triangles": st.triangles, "peel_rounds": st.num_rounds,
+                       "peel_levels": st.num_levels, "parallelism": f"replicas{world}",
+                       "phase_ms": {"build": pm["build"], "support": sup_ms, "peel": pm["peel"]},
                        "peel_phase_ms": st.as_dict()["peel_phase_ms"], "compactions": st.compactions,
-                       "walk_entries": st.walk_entries,
+                       "walk_entries": st.walk_entries, "parity": parity,
                        "replay": {"ms_per_step": replay_ms, "mode": replay_mode,
                                   "how": "kt_engine_replay: the same steps through a CUDA graph of the device "
                                          "pipeline (repeat runs on unchanged input, no host-side input checks)"},
                        "schedule": sched},
+            "single_k3": {"ms": k3_ms, "edges_per_s": m / (k3_ms * 1e-3), "kept_edges": k3_kept,
+                          "how": "kt_engine_ktruss at k = 3 on the same graph (device buffers): the unit the "
+                                 "reference arm times"},
+            "er4096_full_decomposition": {"ms": er_ms, "edges_per_s": len(et) / (er_ms * 1e-3), "m": len(et),
+                                          "k_max": ek},
             "e2e": {"value": replica_throughput(m, world, e2e_s * 1e3), "unit": "edges/s", "h2d_bytes_per_step": 8 * N,
                     "d2h_bytes_per_step": 4 * N, "ms_per_step": e2e_s * 1e3,
                     "last_call_device_ms": {"copy_in": ls.copy_in_ms, "decompose": ls.last_ms,
                                             "copy_out": ls.copy_out_ms}},
-            "gpu_launches": launches // args.steps * args.steps,
+            "gpu_launches": launches,
             "roofline": {"bound": "hbm", "kernel": "k_peel", "achieved": pk_gbs, "peak": hbm,
                          "peak_kind": hbm_kind, "unit": "GB/s", "frac": pk_gbs / hbm,
-                         "traffic": traffic.get("k_peel"), "algorithmic_bytes": plain_bytes,
-                         "kernel_ms": pk_ms, "passes": st.plain_passes, "alive_sum": st.plain_alive_sum},
+                         "traffic": traffic.get("k_peel"), "traffic_source": traffic_note,
+                         "algorithmic_bytes": plain_bytes, "kernel_ms": pk_ms, "passes": passes,
+                         "alive_sum": alive_sum, "passes_source": "oracle fixture" if fx else "engine round log"},
             "roofline_support": {"bound": "hbm", "kernel": "k_support", "achieved": sup_gbs, "peak": hbm,
                                  "unit": "GB/s", "frac": sup_gbs / hbm, "traffic": traffic.get("k_support"),
-                                 "algorithmic_bytes": sup_bytes, "kernel_ms": sup_ms},
+                                 "traffic_source": traffic_note, "algorithmic_bytes": sup_bytes, "kernel_ms": sup_ms},
             "clocks": clk.summary()}
     if rank == 0 and world == 1 and not args.no_cpu:
-        s, rate = cpu_sample(n, src, dst, args.cpu_budget, None)
-    else:
-        rate = None
-    if rate == 0:
-        line["cpu_baseline"] = {"value": None, "unit": "edges/s", "cores": 1, "kind": "port",
-                                "sample": f"no triangle count of the reference's first pass finished its first "
-                                          f"4096 edges within {args.cpu_budget:.0f} s (graph set-up included)"}
-    elif rate:
-        t_full = st.plain_alive_sum / rate
-        line["cpu_baseline"] = {"value": m / t_full, "unit": "edges/s", "cores": 1, "kind": "port",
-                                "sample": (f"first {s['passes']} complete of {st.plain_passes} count-and-prune "
-                                           f"passes of the reference's chained decomposition ({s['alive_sum']} of "
-                                           f"{st.plain_alive_sum} alive-edge visits, a cut pass's merged edges "
-                                           f"included) in {s['seconds']:.1f} s with graph set-up, scaled by "
-                                           f"alive-edge volume")}
+        threads = host_threads()
+        secs, cpasses, kept = k3_runs_cpu(n, src, dst, 1, args.cpu_runs, threads)
+        if kept != k3_kept:
+            raise RuntimeError("CPU and GPU k = 3 truss sizes differ")
+        cms = float(np.mean(secs)) * 1e3
+        line["cpu_baseline"] = {"value": m / (cms * 1e-3), "unit": "edges/s", "cores": threads, "kind": "port",
+                                "sample": (f"{args.cpu_runs} complete single-k runs at k = 3 on the whole graph "
+                                           f"({cms:.0f} ms each; the GPU's time for the same unit is single_k3.ms): "
+                                           "the oracle port of the reference loop, count and mark sweeps on "
+                                           f"{threads} host threads; a complete CPU decomposition of this graph "
+                                           "takes hours")}
     if rank == 0:
         print(json.dumps(line), flush=True)
     eng.close()
@@ -733,8 +911,12 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="rmat20",
                     choices=sorted(WORKLOADS) + sorted(BATCHES) + ["selector", "ingest"])
-    ap.add_argument("--cpu-budget", type=float, default=15.0)
+    ap.add_argument("--cpu-runs", type=int, default=3,
+                    help="cpu_baseline: complete single-k runs at k = 3 timed on the host cores")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--decomposition-estimate", type=int, default=0, metavar="STRATA",
+                    help="reference arm: also estimate the complete CPU decomposition from STRATA complete level "
+                         "runs (an extrapolation, reported apart from value)")
     ap.add_argument("--single-graphs", type=int, default=4096,
                     help="batch workloads: graphs of the batch also decomposed one call each")
     ap.add_argument("--schedule", default=None,

@@ -374,11 +374,14 @@ int kt_engine_selftest_barrier_timeout(kt_engine* engine, uint64_t timeout_ns);
  * memory manager with a fixed budget, and latency-sensitive loops that cannot afford
  * cudaMalloc/cudaFree (which may synchronize the device).  Same inputs and outputs as
  * kt_engine_decompose on the current device and `stream` (a cudaStream_t, NULL = default stream);
- * all scratch lives in a 40 MiB static device array held by every GPU that loads this library
- * until the process exits.  Limits: at most 524,288 entries (262,144 undirected edges) and
- * 131,072 vertices, else KT_ERR_TOO_LARGE.  The first call on a device sets the array up and
- * should happen before any stream capture.  Calls on a device share the array; they are
- * serialized and each returns after its GPU work has finished (overlapping work would race). */
+ * all scratch lives in a 40 MiB static device array, held on every GPU where it is loaded until
+ * the process exits.  CUDA loads modules lazily by default, so the array is usually backed at the
+ * first call on a device (at context creation under CUDA_MODULE_LOADING=EAGER): that first call
+ * can fail with a CUDA error when device memory is short; later calls allocate nothing.  Limits:
+ * at most 524,288 entries (262,144 undirected edges) and 131,072 vertices, else
+ * KT_ERR_TOO_LARGE.  The first call on a device sets the array up and should happen before any
+ * stream capture.  Calls on a device share the array; they are serialized, and each call
+ * synchronizes `stream` before it returns (overlapping work would race). */
 int kt_decompose_noalloc(const uint32_t* d_src, const uint32_t* d_dst, uint64_t num_entries,
                          uint32_t num_nodes, uint32_t* d_truss_per_entry, uint32_t* d_k_max,
                          void* stream);

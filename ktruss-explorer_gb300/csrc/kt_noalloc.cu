@@ -9,15 +9,21 @@
 // from one statically sized device array declared below.  The caller passes device buffers for
 // the input entries and the outputs.
 //
-// The array costs kNoAllocScratchBytes of device memory on every GPU that loads the library,
-// from module load until the process exits, whether or not the entry point is used.
+// The array costs kNoAllocScratchBytes of device memory on every GPU where it is loaded, until
+// the process exits.  CUDA loads modules lazily by default, so the array is usually backed when
+// the first call on a device takes its address (or when the context is created, under
+// CUDA_MODULE_LOADING=EAGER): that first call can fail with a CUDA error when device memory is
+// short.  Later calls allocate nothing.
 //
 // Set-up: the first call on a device (with that device current) takes the array's device address
 // with cudaGetSymbolAddress and lays the workspace out in it; that first call should happen before
-// any stream capture.  All calls on a device share the array, which keeps the previous call's
-// contents; the pipeline clears what must start at zero (control words, degrees, supports, round
-// stamps).  Calls on one device are serialized by a lock and each returns only after its own GPU
-// work has finished: two calls whose GPU work overlapped would race on the shared scratch.
+// any stream capture.  Every later call looks the address up again (a host-side lookup): if the
+// context was torn down and made again (cudaDeviceReset), the module is reloaded and the array may
+// have moved, and the workspace is laid out again at the new address.  All calls on a device share
+// the array, which keeps the previous call's contents; the pipeline clears what must start at zero
+// (control words, degrees, supports, round stamps).  Calls on one device are serialized by a lock,
+// and each call synchronizes its stream before it returns: two calls whose GPU work overlapped
+// would race on the shared scratch.
 
 #include <mutex>
 
@@ -40,18 +46,16 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratch
 struct NoAllocDevice {
     std::mutex mu;
     bool ready = false;
+    void* base = nullptr;               // the array's device address at the last set-up
     kt_engine engine;                   // pointers carved from g_noalloc_scratch; no events, no arena
     uint32_t h_ctrl[kt::kCtrlWords];    // host copy of the control words (static, not pinned)
 };
 
 NoAllocDevice g_devices[kMaxDevices];
 
-// Once per device, with the device current: the array's address and the workspace layout.
-int set_up(int device, NoAllocDevice& d) {
-    void* ptr = nullptr;
-    int rc = kt::check_cuda(cudaGetSymbolAddress(&ptr, g_noalloc_scratch),
-                            "cudaGetSymbolAddress of the no-allocation scratch");
-    if (rc) return rc;
+// With the device current: the workspace layout inside the array at device address `ptr`.
+int set_up(int device, NoAllocDevice& d, void* ptr) {
+    int rc;
     kt_engine& e = d.engine;
     e.device = device;
     if ((rc = kt::check_cuda(cudaDeviceGetAttribute(&e.num_sms, cudaDevAttrMultiProcessorCount, device),
@@ -66,6 +70,7 @@ int set_up(int device, NoAllocDevice& d) {
     e.cap_nodes = kNoAllocMaxNodes;
     e.cap_entries = kNoAllocMaxEntries;
     e.h_ctrl = d.h_ctrl;
+    d.base = ptr;
     d.ready = true;
     return KT_OK;
 }
@@ -90,7 +95,12 @@ extern "C" int kt_decompose_noalloc(const uint32_t* d_src, const uint32_t* d_dst
     if (device < 0 || device >= kMaxDevices) return kt::fail(KT_ERR_NO_DEVICE, "device %d out of range", device);
     NoAllocDevice& d = g_devices[device];
     std::lock_guard<std::mutex> lock(d.mu);
-    if (!d.ready && (rc = set_up(device, d))) return rc;
+    // the array's address on every call: a context made again after a reset may have moved it
+    void* ptr = nullptr;
+    if ((rc = kt::check_cuda(cudaGetSymbolAddress(&ptr, g_noalloc_scratch),
+                             "cudaGetSymbolAddress of the no-allocation scratch")))
+        return rc;
+    if ((!d.ready || ptr != d.base) && (rc = set_up(device, d, ptr))) return rc;
     kt_engine& e = d.engine;
     e.stream = static_cast<cudaStream_t>(stream);
     e.stats_ready = false;

@@ -31,7 +31,19 @@ typedef struct ko_pass_log {
     uint32_t cap;
     uint32_t num;
     uint64_t* alive;
+    double loop_seconds; /* wall time of the count-and-prune loop alone: the span the reference's
+                            k-truss timer covers (kernel_hdc.cu:213-229), without relabel and CSR build */
 } ko_pass_log;
+
+/* Per-level pass statistics of the reference chain, indexed by k: passes[k] count-and-prune
+ * passes of the single-k run at k (on the (k-1)-truss), alive[k] the sum of their alive oriented
+ * edge counts.  num = largest stored k + 1. */
+typedef struct ko_level_log {
+    uint32_t cap;
+    uint32_t num;
+    uint32_t* passes;
+    uint64_t* alive;
+} ko_level_log;
 
 /* Single-k k-truss (kernel.cu:9-39 -> kernel_h.cu:11-68 -> kernel_h{d,u}c.cu).
  * Writes the surviving edges in both directions to out_src/out_dst (capacity num_entries)
@@ -61,6 +73,37 @@ int ko_chain_sample(uint32_t num_nodes, uint32_t num_entries, const uint32_t* sr
 int ko_decompose_peel(uint32_t num_nodes, uint32_t num_entries, const uint32_t* src,
                       const uint32_t* dst, uint32_t* truss_per_entry, uint32_t* k_max,
                       uint32_t* plain_passes, uint64_t* plain_alive_sum, uint32_t* num_rounds);
+
+/* ko_decompose_peel with the per-level pass statistics of the reference chain (levels may be
+ * NULL). */
+int ko_decompose_peel_levels(uint32_t num_nodes, uint32_t num_entries, const uint32_t* src,
+                             const uint32_t* dst, uint32_t* truss_per_entry, uint32_t* k_max,
+                             uint32_t* plain_passes, uint64_t* plain_alive_sum, uint32_t* num_rounds,
+                             ko_level_log* levels);
+
+/* ko_decompose_peel_levels with its phases split over `threads` host threads: the same outputs
+ * (the rounds are the same synchronous rounds; only the work inside each is shared). */
+int ko_decompose_peel_mt(uint32_t num_nodes, uint32_t num_entries, const uint32_t* src,
+                         const uint32_t* dst, uint32_t* truss_per_entry, uint32_t* k_max,
+                         uint32_t* plain_passes, uint64_t* plain_alive_sum, uint32_t* num_rounds,
+                         ko_level_log* levels, uint32_t threads);
+
+/* Repeat runs of the reference's single-k loop (default variant: directed by degree, recount all,
+ * no compaction) with its count and mark sweeps split over `threads` host threads: relabel,
+ * orientation and CSR once; each of `runs` runs restores the CSR and times the count-and-prune
+ * loop alone (run_seconds[i], run_passes[i]).  Writes the last run's truss edges (both
+ * directions) like ko_ktruss.  Returns 0, or -1 on an allocation failure. */
+int ko_ktruss_runs(uint32_t num_nodes, uint32_t num_entries, const uint32_t* src, const uint32_t* dst,
+                   uint32_t k, uint32_t runs, uint32_t threads, uint32_t* out_src, uint32_t* out_dst,
+                   uint32_t* out_num, double* run_seconds, uint32_t* run_passes);
+
+/* R-MAT generator: the same graph as the engine's kt_gen_rmat for the same arguments (a
+ * restatement of that seeded generator, so that the CPU baseline makes its input without the
+ * product library).  Writes the canonical edges u < v sorted by (u, v), without duplicates or
+ * self loops, into u/v (capacity edge_factor << scale) and their count to *num_edges.
+ * Returns 0, or -1 on bad arguments or an allocation failure. */
+int ko_gen_rmat(uint32_t scale, uint32_t edge_factor, double a, double b, double c, uint64_t seed,
+                uint32_t* u, uint32_t* v, uint64_t* num_edges);
 
 #ifdef __cplusplus
 }

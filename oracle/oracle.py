@@ -24,7 +24,13 @@ _lib = None
 
 
 class _PassLog(ctypes.Structure):
-    _fields_ = [("cap", ctypes.c_uint32), ("num", ctypes.c_uint32), ("alive", ctypes.POINTER(ctypes.c_uint64))]
+    _fields_ = [("cap", ctypes.c_uint32), ("num", ctypes.c_uint32), ("alive", ctypes.POINTER(ctypes.c_uint64)),
+                ("loop_seconds", ctypes.c_double)]
+
+
+class _LevelLog(ctypes.Structure):
+    _fields_ = [("cap", ctypes.c_uint32), ("num", ctypes.c_uint32), ("passes", ctypes.POINTER(ctypes.c_uint32)),
+                ("alive", ctypes.POINTER(ctypes.c_uint64))]
 
 
 def build() -> str:
@@ -49,6 +55,15 @@ def _load():
                                         ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_double)]
         lib.ko_decompose_peel.argtypes = [ctypes.c_uint32, ctypes.c_uint32, u32p, u32p, u32p, u32p, u32p,
                                           ctypes.POINTER(ctypes.c_uint64), u32p]
+        lib.ko_decompose_peel_levels.argtypes = [ctypes.c_uint32, ctypes.c_uint32, u32p, u32p, u32p, u32p, u32p,
+                                                 ctypes.POINTER(ctypes.c_uint64), u32p, ctypes.POINTER(_LevelLog)]
+        lib.ko_decompose_peel_mt.argtypes = [ctypes.c_uint32, ctypes.c_uint32, u32p, u32p, u32p, u32p, u32p,
+                                             ctypes.POINTER(ctypes.c_uint64), u32p, ctypes.POINTER(_LevelLog),
+                                             ctypes.c_uint32]
+        lib.ko_ktruss_runs.argtypes = [ctypes.c_uint32, ctypes.c_uint32, u32p, u32p, ctypes.c_uint32, ctypes.c_uint32,
+                                       ctypes.c_uint32, u32p, u32p, u32p, ctypes.POINTER(ctypes.c_double), u32p]
+        lib.ko_gen_rmat.argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_double, ctypes.c_double,
+                                    ctypes.c_double, ctypes.c_uint64, u32p, u32p, ctypes.POINTER(ctypes.c_uint64)]
         _lib = lib
     return _lib
 
@@ -62,46 +77,117 @@ def _u32(a) -> np.ndarray:
 
 
 def ktruss(num_nodes: int, src, dst, k: int, directedness: int = DIRECTED_BY_DEGREE,
-           recount: int = RECOUNT_ALL, num_edge_remove_iter: int = 0, pass_log: bool = False):
-    """Single-k k-truss (the reference's Host path).  Returns (out_src, out_dst[, alive per pass])."""
+           recount: int = RECOUNT_ALL, num_edge_remove_iter: int = 0, pass_log: bool = False,
+           loop_seconds: bool = False):
+    """Single-k k-truss (the reference's Host path).  Returns (out_src, out_dst[, alive per pass]
+    [, seconds of the count-and-prune loop, the span the reference's k-truss timer covers])."""
     lib = _load()
     src, dst = _u32(src), _u32(dst)
     n = len(src)
     os_, od = np.zeros(max(n, 1), np.uint32), np.zeros(max(n, 1), np.uint32)
     num = ctypes.c_uint32(0)
     alive = np.zeros(1 << 16, np.uint64)
-    log = _PassLog(len(alive), 0, alive.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)))
+    log = _PassLog(len(alive), 0, alive.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)), 0.0)
     rc = lib.ko_ktruss(num_nodes, n, _p(src), _p(dst), k & 0xFFFFFFFF, directedness, recount,
                        num_edge_remove_iter, _p(os_), _p(od), ctypes.byref(num), ctypes.byref(log))
     if rc != 0:
         raise MemoryError("oracle ko_ktruss failed")
     out = (os_[: num.value].copy(), od[: num.value].copy())
     if pass_log:
-        return out + (alive[: min(log.num, len(alive))].copy(),)
+        out = out + (alive[: min(log.num, len(alive))].copy(),)
+    if loop_seconds:
+        out = out + (log.loop_seconds,)
     return out
 
 
-def decompose(num_nodes: int, src, dst, method: str = "peel"):
+def decompose(num_nodes: int, src, dst, method: str = "peel", levels: bool = False, threads=None):
     """Per-entry truss numbers.  method 'chain' chains single-k runs like the reference
-    would be driven; 'peel' is the exact serial peeling.  Returns a dict."""
+    would be driven; 'peel' is the exact peeling (on `threads` host threads; None: one thread
+    below a million entries, else up to 16).  Returns a dict; with levels=True (peel only) also
+    'level_passes' and 'level_alive': per k, the passes of the reference chain's single-k run at k
+    and the sum of their alive oriented edges."""
     lib = _load()
     src, dst = _u32(src), _u32(dst)
     n = len(src)
     truss = np.zeros(max(n, 1), np.uint32)
     kmax, passes, rounds = ctypes.c_uint32(0), ctypes.c_uint32(0), ctypes.c_uint32(0)
     alive_sum = ctypes.c_uint64(0)
+    out = {}
     if method == "chain":
         rc = lib.ko_decompose_chain(num_nodes, n, _p(src), _p(dst), _p(truss), ctypes.byref(kmax),
                                     ctypes.byref(passes), ctypes.byref(alive_sum))
     elif method == "peel":
-        rc = lib.ko_decompose_peel(num_nodes, n, _p(src), _p(dst), _p(truss), ctypes.byref(kmax),
-                                   ctypes.byref(passes), ctypes.byref(alive_sum), ctypes.byref(rounds))
+        cap = (1 << 20) if levels else 0
+        lp = np.zeros(max(cap, 1), np.uint32)
+        la = np.zeros(max(cap, 1), np.uint64)
+        log = _LevelLog(cap, 0, lp.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)),
+                        la.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)))
+        if threads is None:
+            threads = 1 if n < 1_000_000 else min(16, os.cpu_count() or 1)
+        if threads > 1:
+            rc = lib.ko_decompose_peel_mt(num_nodes, n, _p(src), _p(dst), _p(truss), ctypes.byref(kmax),
+                                          ctypes.byref(passes), ctypes.byref(alive_sum), ctypes.byref(rounds),
+                                          ctypes.byref(log) if levels else None, threads)
+        else:
+            rc = lib.ko_decompose_peel_levels(num_nodes, n, _p(src), _p(dst), _p(truss), ctypes.byref(kmax),
+                                              ctypes.byref(passes), ctypes.byref(alive_sum), ctypes.byref(rounds),
+                                              ctypes.byref(log) if levels else None)
+        if levels:
+            out = {"level_passes": lp[: log.num].copy(), "level_alive": la[: log.num].copy()}
     else:
         raise ValueError(method)
     if rc != 0:
         raise MemoryError("oracle decomposition failed")
     return {"truss": truss[:n].copy(), "k_max": kmax.value, "plain_passes": passes.value,
-            "plain_alive_sum": alive_sum.value, "rounds": rounds.value if method == "peel" else None}
+            "plain_alive_sum": alive_sum.value, "rounds": rounds.value if method == "peel" else None, **out}
+
+
+def ktruss_runs(num_nodes: int, src, dst, k: int, runs: int, threads: int = 0):
+    """Repeat runs of the reference's single-k loop (directed by degree, recount all) on `threads`
+    host threads (0: all, at most 64): the CSR is built once, each run restores it and times the
+    count-and-prune loop alone, like the reference's -w/-x runs.  Returns (out_src, out_dst of the
+    last run, seconds per run, passes per run)."""
+    lib = _load()
+    src, dst = _u32(src), _u32(dst)
+    n = len(src)
+    threads = threads or min(64, os.cpu_count() or 1)
+    os_, od = np.zeros(max(n, 1), np.uint32), np.zeros(max(n, 1), np.uint32)
+    num = ctypes.c_uint32(0)
+    secs = np.zeros(max(runs, 1), np.float64)
+    passes = np.zeros(max(runs, 1), np.uint32)
+    rc = lib.ko_ktruss_runs(num_nodes, n, _p(src), _p(dst), k & 0xFFFFFFFF, runs, threads, _p(os_), _p(od),
+                            ctypes.byref(num), secs.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), _p(passes))
+    if rc != 0:
+        raise MemoryError("oracle ko_ktruss_runs failed")
+    return os_[: num.value].copy(), od[: num.value].copy(), secs[:runs].copy(), passes[:runs].copy()
+
+
+def _peel_job(job):
+    n, src, dst = job
+    r = decompose(n, src, dst, method="peel", threads=1)
+    return r["truss"], r["k_max"]
+
+
+def decompose_many(jobs, workers: int = 0):
+    """Peel decompositions of many graphs [(num_nodes, src, dst), ...] in a process pool started
+    with spawn (safe to start after CUDA was initialised in the caller).  Returns [(truss, k_max)]."""
+    import multiprocessing as mp
+
+    workers = workers or min(16, mp.cpu_count())
+    with mp.get_context("spawn").Pool(workers) as pool:
+        return pool.map(_peel_job, jobs, chunksize=1)
+
+
+def gen_rmat(scale: int, edge_factor: int, a: float = 0.57, b: float = 0.19, c: float = 0.19, seed: int = 1):
+    """R-MAT graph of the engine's generator (same arguments, same edges), made without the product
+    library.  Returns (num_nodes, u, v): canonical edges u < v sorted by (u, v)."""
+    lib = _load()
+    cap = edge_factor << scale
+    u, v = np.zeros(cap, np.uint32), np.zeros(cap, np.uint32)
+    num = ctypes.c_uint64(0)
+    if lib.ko_gen_rmat(scale, edge_factor, a, b, c, seed, _p(u), _p(v), ctypes.byref(num)) != 0:
+        raise ValueError("oracle ko_gen_rmat: bad arguments or out of memory")
+    return 1 << scale, u[: num.value].copy(), v[: num.value].copy()
 
 
 def chain_sample(num_nodes: int, src, dst, budget_s: float) -> dict:

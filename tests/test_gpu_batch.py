@@ -26,6 +26,31 @@ def _per_graph_oracle(n, u, v, off):
     return truss, kmax
 
 
+def test_benchmarked_batch_sample_matches_oracle():
+    """The benchmarked batch itself (4096 graphs, n log-uniform in [500, 50000], half Barabasi-Albert,
+    half Watts-Strogatz, 0-3 planted cliques of 8-64 vertices, seed 1), decomposed in one call; 96
+    graphs spread over it (every 43rd) are checked against the oracle, which runs in a process pool
+    started with spawn."""
+    n, u, v, off = kt.gen_batch(4096, 500, 50000, 1)
+    src, dst = both_directions(u, v)
+    truss, kmax = kt.decompose_batch(src, dst, n, off)
+    m = len(u)
+    pick = np.arange(0, 4096, 43)
+    lo = np.searchsorted(u, off[pick], side="left")
+    hi = np.searchsorted(u, off[pick + 1], side="left")
+    jobs = []
+    for g, a, b in zip(pick, lo, hi):
+        lu, lv = u[a:b] - off[g], v[a:b] - off[g]
+        s, d = both_directions(lu, lv)
+        jobs.append((int(off[g + 1] - off[g]), s, d))
+    assert max(j[0] for j in jobs) > 25000 and sum(len(j[1]) for j in jobs) > 4_000_000
+    results = oracle.decompose_many(jobs)
+    for (g, a, b), (t_ref, k_ref) in zip(zip(pick, lo, hi), results):
+        assert kmax[g] == k_ref, f"graph {g}: k_max {kmax[g]} != {k_ref}"
+        assert np.array_equal(truss[a:b], t_ref[: b - a]), f"graph {g}: truss numbers differ"
+        assert np.array_equal(truss[m + a:m + b], t_ref[: b - a]), f"graph {g}: reverse entries differ"
+
+
 @pytest.mark.parametrize("seed", [5, 6])
 def test_batch_matches_each_graph(seed):
     n, u, v, off = kt.gen_batch(48, 64, 2500, seed)

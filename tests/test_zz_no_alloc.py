@@ -42,6 +42,33 @@ def test_noalloc_matches_engine_on_consecutive_calls():
     eng.close()
 
 
+def test_noalloc_calls_allocate_no_device_memory():
+    """After a first round of calls (which backs the static array and loads every kernel the calls
+    use), further calls on graphs of different sizes leave the device's free memory unchanged."""
+    torch = pytest.importorskip("torch")
+    bufs = []
+    for n, u, v in _graphs():
+        src, dst = both_directions(u, v)
+        out = torch.zeros(len(src), dtype=torch.int32, device="cuda")
+        out_k = torch.zeros(1, dtype=torch.int32, device="cuda")
+        bufs.append((n, len(src), _device(torch, src), _device(torch, dst), out, out_k))
+    torch.cuda.synchronize()
+
+    def call(b):
+        n, N, d_src, d_dst, out, out_k = b
+        kt.decompose_noalloc(d_src.data_ptr(), d_dst.data_ptr(), N, n, out.data_ptr(), out_k.data_ptr())
+
+    for b in bufs:
+        call(b)
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for b in bufs[::-1] + bufs:
+        call(b)
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0, f"free device memory changed by {free0 - free1} bytes"
+
+
 def test_noalloc_rejects_graphs_beyond_its_scratch():
     torch = pytest.importorskip("torch")
     d = torch.zeros(4, dtype=torch.int32, device="cuda")
