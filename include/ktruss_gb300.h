@@ -188,7 +188,8 @@ typedef struct kt_stats {
 /* Schedule of the engine's kernels (no counterpart in the reference, whose tuning knobs are the
  * -b/-t block and tile sizes).  Every schedule gives the same result; only the time differs. */
 typedef struct kt_schedule {
-    uint32_t support_group;    /* lanes per oriented edge in the support count: 4, 8, 16 or 32   */
+    uint32_t support_group;    /* support count: lanes per oriented edge (4, 8, 16 or 32), or 0
+                                  for the vertex-centric count with shared-memory hash tables   */
     uint32_t chunk_width;      /* row entries per peel work chunk (lanes per chunk): 8, 16 or 32  */
     uint32_t compact_percent;  /* compact the adjacency rows at a level start once the alive
                                   edges are below this percentage of the count at the last
@@ -268,6 +269,14 @@ int kt_engine_level_log(kt_engine* engine, uint32_t* k, uint32_t* alive, uint32_
  * ranges above); kt_engine_get_schedule reads it. */
 int kt_engine_set_schedule(kt_engine* engine, const kt_schedule* schedule);
 int kt_engine_get_schedule(kt_engine* engine, kt_schedule* schedule);
+
+/* Wait limit of the peel kernel's grid barriers (no counterpart in the reference, whose loop is
+ * driven from the host): every wait is bounded by base_ns plus ns_per_unit for each unit of work
+ * the wait can legitimately cover - each row entry queued for the round that the barrier closes,
+ * each edge (twice) for a level phase - after which the kernel returns KT_ERR_TIMEOUT instead of
+ * waiting forever.  Defaults: 10 s and 8 ns.  base_ns must be at least 1 microsecond. */
+int kt_engine_set_wait_limit(kt_engine* engine, uint64_t base_ns, uint32_t ns_per_unit);
+int kt_engine_get_wait_limit(kt_engine* engine, uint64_t* base_ns, uint32_t* ns_per_unit);
 /* Statistics of the last call of the host-buffer entry points (kt_ktruss, kt_decompose,
  * kt_decompose_batch), including the device time of their copies (copy_in_ms, copy_out_ms). */
 int kt_last_stats(kt_stats* stats);

@@ -25,15 +25,15 @@ enum : uint32_t {
 // Layout of the device control block (uint32 words unless noted).
 enum : uint32_t {
     kCtrlError = 0,
-    // words 1-9, 12, 13 and 21-27 are unused
+    // words 1, 12, 13 and 21-27 are unused
+    kPRoundWalk = 2,      // [4] u64 (words 2..9): row entries queued for the round (wait limits)
     kCtrlTriLo = 10,      // 64-bit triangle counter (lo, hi)
     kCtrlTriHi = 11,
     kCtrlBigRow = 14,     // first rank whose symmetric row is long (block-wide compaction)
     kCtrlTinyRow = 15,    // first rank whose symmetric row is not tiny (thread-wise compaction below)
     // Persistent peel kernel: barrier, outputs, and rings of per-round / per-level counters
     // (slot r % 4 belongs to round r; slot (r+2) % 4 is cleared during round r).
-    kPBarCount = 16,
-    kPBarGen = 17,
+    kPBarCount = 16,   // u64 (words 16..17): grid-barrier arrivals since the launch
     kPKmax = 18,
     kPRounds = 19,
     kPLevels = 20,
@@ -137,40 +137,44 @@ __device__ __forceinline__ uint64_t global_ns() {
     return t;
 }
 
+__device__ __forceinline__ unsigned long long atom_add_acq_rel_u64(unsigned long long* p, unsigned long long v) {
+    unsigned long long old;
+    asm volatile("atom.add.acq_rel.gpu.global.u64 %0, [%1], %2;" : "=l"(old) : "l"(p), "l"(v) : "memory");
+    return old;
+}
+
 // Grid-wide barrier for a cooperative launch whose `expected` blocks are all resident.
-// Every wait is bounded: a block that waits longer than timeout_ns sets kErrTimeout in
-// ctrl[kCtrlError] and returns false; blocks that see the bit return false too, so the
-// kernel ends instead of hanging.  Returns true when all blocks arrived.
+// One 64-bit arrival counter, never reset during a launch: after the block's threads meet at
+// __syncthreads, thread 0 adds 1 with acquire-release semantics (its block's writes become
+// visible to whoever acquires the counter) and, unless it completed the barrier, polls the
+// counter with acquire loads until it reaches the next multiple of `expected`.  No generation
+// word, no reset and no fences: the last arriver has nothing to publish.  Every wait is bounded:
+// a block that waits longer than timeout_ns sets kErrTimeout in ctrl[kCtrlError] and returns
+// false; blocks see the bit while they poll and return false too, so the kernel ends instead of
+// hanging.  Returns true when all blocks arrived.  The counter (ctrl words kPBarCount) must be
+// zero at launch.
 __device__ __forceinline__ bool grid_barrier(uint32_t* ctrl, uint32_t expected, uint64_t timeout_ns) {
     __shared__ uint32_t s_ok;
     __syncthreads();
     if (threadIdx.x == 0) {
-        uint32_t ok = (ld_acquire(ctrl + kCtrlError) & kErrTimeout) ? 0u : 1u;
-        if (ok) {
-            uint32_t* gen = ctrl + kPBarGen;
-            const uint32_t g = ld_acquire(gen);
-            __threadfence();
-            if (atomicAdd(ctrl + kPBarCount, 1u) + 1 == expected) {
-                atomicExch(ctrl + kPBarCount, 0u);
-                __threadfence();
-                st_release(gen, g + 1);
-            } else {
-                const uint64_t t0 = global_ns();
-                uint32_t spins = 0, ns = 32;
-                while (ld_acquire(gen) == g) {
+        uint32_t ok = 1;
+        unsigned long long* count = reinterpret_cast<unsigned long long*>(ctrl + kPBarCount);
+        const unsigned long long old = atom_add_acq_rel_u64(count, 1ull);
+        const unsigned long long target = (old / expected + 1) * expected;
+        if (old + 1 != target) {
+            const uint64_t t0 = global_ns();
+            uint32_t spins = 0;
+            while (ld_acquire_u64(count) < target) {
+                if ((++spins & 31u) == 0) {
                     if (ld_acquire(ctrl + kCtrlError) & kErrTimeout) { ok = 0; break; }
                     if (global_ns() - t0 > timeout_ns) {
                         atomicOr(ctrl + kCtrlError, kErrTimeout);
                         ok = 0;
                         break;
                     }
-                    if (++spins > 64) {
-                        __nanosleep(ns);
-                        if (ns < 256) ns <<= 1;
-                    }
+                    if (spins > 256) __nanosleep(64);
                 }
             }
-            __threadfence();
         }
         s_ok = ok;
     }

@@ -447,8 +447,8 @@ int kt_engine_set_schedule(kt_engine* e, const kt_schedule* s) {
     kt::clear_error();
     if (!e || !s) return fail(KT_ERR_INVALID_ARG, "kt_engine_set_schedule: null argument");
     const uint32_t g = s->support_group, w = s->chunk_width;
-    if (g != 4 && g != 8 && g != 16 && g != 32)
-        return fail(KT_ERR_INVALID_ARG, "support_group must be 4, 8, 16 or 32 (got %u)", g);
+    if (g != 0 && g != 4 && g != 8 && g != 16 && g != 32)
+        return fail(KT_ERR_INVALID_ARG, "support_group must be 0 (vertex hash), 4, 8, 16 or 32 (got %u)", g);
     if (w != 8 && w != 16 && w != 32) return fail(KT_ERR_INVALID_ARG, "chunk_width must be 8, 16 or 32 (got %u)", w);
     if (s->compact_percent > 99)
         return fail(KT_ERR_INVALID_ARG, "compact_percent must be 0..99 (got %u)", s->compact_percent);
@@ -457,6 +457,24 @@ int kt_engine_set_schedule(kt_engine* e, const kt_schedule* s) {
     if (s->peel_blocks > 2) return fail(KT_ERR_INVALID_ARG, "peel_blocks must be 0, 1 or 2 (got %u)", s->peel_blocks);
     e->sched = *s;
     kt::drop_replay(e);  // a replay captures the pipeline again with this schedule
+    return KT_OK;
+}
+
+int kt_engine_set_wait_limit(kt_engine* e, uint64_t base_ns, uint32_t ns_per_unit) {
+    kt::clear_error();
+    if (!e) return fail(KT_ERR_INVALID_ARG, "kt_engine_set_wait_limit: null engine");
+    if (base_ns < 1000) return fail(KT_ERR_INVALID_ARG, "kt_engine_set_wait_limit: base below 1 microsecond");
+    e->wait_base_ns = base_ns;
+    e->wait_ns_per_unit = ns_per_unit;
+    kt::drop_replay(e);  // a captured pipeline holds the old limits
+    return KT_OK;
+}
+
+int kt_engine_get_wait_limit(kt_engine* e, uint64_t* base_ns, uint32_t* ns_per_unit) {
+    kt::clear_error();
+    if (!e || !base_ns || !ns_per_unit) return fail(KT_ERR_INVALID_ARG, "kt_engine_get_wait_limit: null argument");
+    *base_ns = e->wait_base_ns;
+    *ns_per_unit = (uint32_t)e->wait_ns_per_unit;
     return KT_OK;
 }
 

@@ -89,6 +89,8 @@ struct kt_engine {
     uint32_t vb = 1;  // bits per rank in sort keys
 
     kt_schedule sched{8, 32, 85, 50, 0};  // kernel schedule (kt_engine_set_schedule)
+    uint64_t wait_base_ns = 10ull * 1000 * 1000 * 1000;  // peel barrier wait limit: base ...
+    uint64_t wait_ns_per_unit = 8;                        // ... plus per unit of covered work
     bool batch_call = false;           // the current call decomposes a batch of separate graphs
     kt_selector* selector = nullptr;   // learned schedule selector (kt_engine_set_selector)
     uint32_t* sel_stats = nullptr;     // 16 u64 graph statistics for the selector's features

@@ -33,8 +33,11 @@
 // Symmetric rows are compacted in place at a level start once enough edges have been removed
 // since the last compaction, so the walks see few removed entries.
 //
-// Every grid barrier wait is bounded (kPeelTimeoutNs); on expiry the kernel reports
-// KT_ERR_TIMEOUT through the control block and returns.
+// Every grid barrier wait is bounded: by the engine's base limit (kt_engine_set_wait_limit, 10 s by
+// default) plus a share proportional to the work the wait can legitimately cover - per row entry
+// queued for the round that the barrier closes, per edge for the level phases (scans, compaction,
+// recount) - so a long legitimate round on a large graph is not cut short.  On expiry the kernel
+// reports KT_ERR_TIMEOUT through the control block and returns.
 
 #include <cstdlib>
 #include <vector>
@@ -51,7 +54,6 @@ constexpr int kThreads = 256;          // helper kernels
 #define KT_PEEL_THREADS 1024
 #endif
 constexpr int kPeelThreads = KT_PEEL_THREADS;  // persistent kernel: one or two blocks per SM
-constexpr uint64_t kPeelTimeoutNs = 10ull * 1000 * 1000 * 1000;
 
 inline uint32_t grid_for(uint64_t n, int threads = kThreads) {
     uint64_t b = (n + threads - 1) / threads;
@@ -90,7 +92,8 @@ struct PeelParams {
     uint32_t recount_num;  // a round whose frontier holds >= recount_num % of the alive edges
                            // recounts the survivors' support instead of decrementing (0: never)
     uint32_t single_k;  // 0: full decomposition; >= 3: the k of a single-k truss
-    uint64_t timeout_ns;
+    uint64_t wait_base_ns;      // wait limit of every grid barrier: base ...
+    uint64_t wait_ns_per_unit;  // ... plus this per unit of work the wait covers
 };
 
 constexpr uint32_t kDead = 0xffffffffu;  // support of a removed edge
@@ -137,6 +140,7 @@ __device__ __forceinline__ void push_edges(const PeelParams& P, uint32_t e, bool
         cb = atomicAdd(reinterpret_cast<unsigned long long*>(P.ctrl + kPChunks) + slot, (unsigned long long)total);
         atomicAdd(P.ctrl + kPEdges + slot, __popc(mt));
         atomicAdd(reinterpret_cast<unsigned long long*>(P.ctrl + kPWalk), (unsigned long long)walked);
+        atomicAdd(reinterpret_cast<unsigned long long*>(P.ctrl + kPRoundWalk) + slot, (unsigned long long)walked);
     }
     cb = __shfl_sync(kFullMask, cb, 0);
     uint4* ch = P.ch[rr & 1];
@@ -406,15 +410,16 @@ __global__ void __launch_bounds__(kPeelThreads, kBlocksPerSm) k_peel(PeelParams 
     unsigned long long* chunk_ctr = reinterpret_cast<unsigned long long*>(ctrl + kPChunks);
     const uint32_t nblocks = gridDim.x;
     const uint32_t lane = lane_id();
-    const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const uint64_t nthreads = (uint64_t)gridDim.x * blockDim.x;
-    const uint32_t gwarp = (uint32_t)(tid >> 5);
-    const uint32_t nwarps = (uint32_t)(nthreads >> 5);
+    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;  // grids of at most 2^20 threads
+    const uint32_t nthreads = gridDim.x * blockDim.x;
+    const uint32_t gwarp = tid >> 5;
+    const uint32_t nwarps = nthreads >> 5;
     const bool leader = blockIdx.x == 0 && threadIdx.x == 0;
 
     // phase clock (block 0, thread 0): time from the previous barrier to the end of this one,
     // kept in shared memory so that it costs the other threads no registers
-    __shared__ unsigned long long phase_ns[7];  // [6] = time of the last phase boundary
+    __shared__ unsigned long long phase_ns[9];  // [6] = time of the last phase boundary,
+                                                // [7] = start of the level, [8] = start of the round
     if (leader) {
         for (int i = 0; i < 6; ++i) phase_ns[i] = 0;
         phase_ns[6] = global_ns();
@@ -427,36 +432,41 @@ __global__ void __launch_bounds__(kPeelThreads, kBlocksPerSm) k_peel(PeelParams 
         phase_ns[6] = now_;                              \
     }
 
+    // wait limits: level phases (scans, compaction, recount) cover work proportional to the edges;
+    // a round's closing barrier covers the row entries queued for the round (read at its start)
+    const uint64_t phase_wait = P.wait_base_ns + P.wait_ns_per_unit * 2ull * P.m;
+    unsigned long long* round_walk = reinterpret_cast<unsigned long long*>(ctrl + kPRoundWalk);
     for (uint64_t j = tid; j < P.m; j += nthreads) {
         P.rnd[j] = 0;
         P.tr[j] = 0;
     }
-    if (!grid_barrier(ctrl, nblocks, P.timeout_ns)) return;
+    if (!grid_barrier(ctrl, nblocks, phase_wait)) return;
     KT_PHASE(0)
 
     // r: stamp of the last round run.  A level's first round skips one stamp: the blocks still
     // reading the previous level's exit test look at ring slot (r+1) & 3, so the new level's
     // first frontier goes to slot (r+2) & 3.  `rounds` counts the rounds actually run.
     uint32_t r = 0, rounds = 0, level = 0, k = 3, k_last = 2;
-    uint64_t live = P.m, live_at_compaction = P.m;
-    const uint64_t max_stamp = 2ull * P.m + 8;
+    uint32_t live = P.m, live_at_compaction = P.m;  // alive edges now and at the last compaction
+#define KT_MAX_STAMP (2ull * P.m + 8)
     for (;;) {
         const uint32_t ls = level & 3;
-        const unsigned long long level_t0 = leader ? global_ns() : 0ull;
+        if (leader) phase_ns[7] = global_ns();
         r += 1;                     // skipped stamp
         const uint32_t rr = r + 1;  // stamp of this level's first round
-        if (level > P.m + 1 || rr > max_stamp) {
+        if (level > P.m + 1 || rr > KT_MAX_STAMP) {
             if (leader) atomicOr(ctrl + kCtrlError, kErrRunaway);
             return;
         }
         if (leader) {
             chunk_ctr[(rr + 1) & 3] = 0;
+            round_walk[(rr + 1) & 3] = 0;
             ctrl[kPBigCount + ((rr + 1) & 3)] = ctrl[kPEdges + ((rr + 1) & 3)] = 0;
         }
         // compact the rows once the alive edges have dropped enough since the last compaction
-        if (live * 100 < live_at_compaction * P.compact_num) {
+        if ((uint64_t)live * 100 < (uint64_t)live_at_compaction * P.compact_num) {
             compact_rows(P, r, warp_cnt);
-            if (!grid_barrier(ctrl, nblocks, P.timeout_ns)) return;
+            if (!grid_barrier(ctrl, nblocks, phase_wait)) return;
             KT_PHASE(3)
             ++compactions;
             live_at_compaction = live;
@@ -512,20 +522,20 @@ __global__ void __launch_bounds__(kPeelThreads, kBlocksPerSm) k_peel(PeelParams 
                 if (mn != kDead) atomicMin(ctrl + kPLMin + ls, mn);
                 if (min_id != kDead) atomicMin(ctrl + kPLMinId + ls, min_id);
             }
-            if (!grid_barrier(ctrl, nblocks, P.timeout_ns)) return;
+            if (!grid_barrier(ctrl, nblocks, phase_wait)) return;
             KT_PHASE(1)
             if (ld_acquire(ctrl + kPLAlive + ls) == 0) break;
             k = ld_acquire(ctrl + kPLMin + ls) + 3;
             lvl_start = ld_acquire(ctrl + kPLMinId + ls);
             if (k != kg) {
                 collect(P, k - 3, rr, lvl_start, tid, nthreads);
-                if (!grid_barrier(ctrl, nblocks, P.timeout_ns)) return;
+                if (!grid_barrier(ctrl, nblocks, phase_wait)) return;
                 KT_PHASE(2)
             }
         } else {
             k = P.single_k;
             collect(P, k - 3, rr, 0u, tid, nthreads);
-            if (!grid_barrier(ctrl, nblocks, P.timeout_ns)) return;
+            if (!grid_barrier(ctrl, nblocks, phase_wait)) return;
             KT_PHASE(2)
         }
         const uint32_t km2 = k - 2;
@@ -533,20 +543,21 @@ __global__ void __launch_bounds__(kPeelThreads, kBlocksPerSm) k_peel(PeelParams 
         if (leader && level < P.cap_levels) {
             P.level_k[level] = k;
             P.level_alive[level] = P.single_k ? P.m : ld_acquire(ctrl + kPLAlive + ls);
-            P.level_ns[level] = (uint32_t)(global_ns() - level_t0);
+            P.level_ns[level] = (uint32_t)(global_ns() - phase_ns[7]);
             P.level_front[level] = E;
         }
         uint32_t C = (uint32_t)min(ld_acquire_u64(chunk_ctr + (rr & 3)), (unsigned long long)P.cap_chunks);
         while (E) {
             ++r;
             ++rounds;
-            if (r > max_stamp) {
+            if (r > KT_MAX_STAMP) {
                 if (leader) atomicOr(ctrl + kCtrlError, kErrRunaway);
                 return;
             }
             if (leader) {
                 const uint32_t z = (r + 2) & 3;
                 chunk_ctr[z] = 0;
+                round_walk[z] = 0;
                 ctrl[kPBigCount + z] = 0;
                 ctrl[kPEdges + z] = 0;
                 if (rounds < P.cap_rounds) {
@@ -555,7 +566,12 @@ __global__ void __launch_bounds__(kPeelThreads, kBlocksPerSm) k_peel(PeelParams 
                 }
             }
             const bool recount = P.recount_num != 0 && (uint64_t)E * 100 >= (uint64_t)P.recount_num * live;
-            const unsigned long long round_t0 = leader ? phase_ns[6] : 0ull;
+            if (leader) phase_ns[8] = phase_ns[6];
+            // limit of the barrier that closes the round: base + the round's queued row entries
+            const uint64_t round_wait =
+                threadIdx.x == 0 ? (recount ? phase_wait
+                                            : P.wait_base_ns + P.wait_ns_per_unit * ld_acquire_u64(round_walk + (r & 3)))
+                                 : 0;
             if (recount) {
                 // the whole frontier is removed at once (truss number k-1), the support of every
                 // surviving edge is counted again, and the next frontier comes from a scan
@@ -568,10 +584,10 @@ __global__ void __launch_bounds__(kPeelThreads, kBlocksPerSm) k_peel(PeelParams 
                         P.sup[j] = 0;
                     }
                 }
-                if (!grid_barrier(ctrl, nblocks, P.timeout_ns)) return;
+                if (!grid_barrier(ctrl, nblocks, phase_wait)) return;
                 KT_PHASE(4)
                 recount_support(P, lvl_start, tid, nthreads);
-                if (!grid_barrier(ctrl, nblocks, P.timeout_ns)) return;
+                if (!grid_barrier(ctrl, nblocks, phase_wait)) return;
                 KT_PHASE(4)
                 collect(P, k - 3, r + 1, lvl_start, tid, nthreads);
             } else {
@@ -625,8 +641,8 @@ __global__ void __launch_bounds__(kPeelThreads, kBlocksPerSm) k_peel(PeelParams 
                 }
             }
             }
-            if (!grid_barrier(ctrl, nblocks, P.timeout_ns)) return;
-            if (leader && rounds < P.cap_rounds) P.round_ns[rounds] = (uint32_t)(global_ns() - round_t0);
+            if (!grid_barrier(ctrl, nblocks, round_wait)) return;
+            if (leader && rounds < P.cap_rounds) P.round_ns[rounds] = (uint32_t)(global_ns() - phase_ns[8]);
             KT_PHASE(recount ? 4 : 5)
             live -= E;
             E = ld_acquire(ctrl + kPEdges + ((r + 1) & 3));
@@ -648,6 +664,7 @@ __global__ void __launch_bounds__(kPeelThreads, kBlocksPerSm) k_peel(PeelParams 
         }
     }
 #undef KT_PHASE
+#undef KT_MAX_STAMP
 }
 
 // A barrier that cannot complete (it expects one block more than the grid has): every wait
@@ -658,7 +675,7 @@ __global__ void k_barrier_probe(uint32_t* ctrl, uint64_t timeout_ns) {
 
 __global__ void k_init_peel_ctrl(uint32_t* ctrl) {
     const uint32_t i = threadIdx.x;
-    if (i >= kPBarCount && i < kCtrlWords)
+    if ((i >= kPBarCount && i < kCtrlWords) || (i >= kPRoundWalk && i < kPRoundWalk + 8))
         ctrl[i] = (i >= kPLMin && i < kPLMin + 4) || (i >= kPLMinId && i < kPLMinId + 4) ? 0xffffffffu : 0u;
 }
 
@@ -778,7 +795,8 @@ int launch_peel(kt_engine* e, uint32_t single_k) {
     P.compact_num = e->sched.compact_percent;
     P.recount_num = e->sched.recount_percent;
     P.single_k = single_k;
-    P.timeout_ns = kPeelTimeoutNs;
+    P.wait_base_ns = e->wait_base_ns;
+    P.wait_ns_per_unit = e->wait_ns_per_unit;
     void* args[] = {&P};
     const bool timed = e->ev_peel0 && e->ev_peel1 && !e->trusted;
     if (timed && (rc = check_cuda(cudaEventRecord(e->ev_peel0, e->stream), "record event"))) return rc;

@@ -149,6 +149,8 @@ def lib() -> ctypes.CDLL:
         L.kt_schedule_default.argtypes = []
         L.kt_engine_set_schedule.argtypes = [_VP, ctypes.POINTER(Schedule)]
         L.kt_engine_get_schedule.argtypes = [_VP, ctypes.POINTER(Schedule)]
+        L.kt_engine_set_wait_limit.argtypes = [_VP, ctypes.c_uint64, ctypes.c_uint32]
+        L.kt_engine_get_wait_limit.argtypes = [_VP, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint32)]
         _FP = ctypes.POINTER(ctypes.c_float)
         L.kt_selector_create.argtypes = [ctypes.c_int, ctypes.c_uint64, ctypes.POINTER(_VP)]
         L.kt_selector_destroy.argtypes = [_VP]
@@ -402,6 +404,15 @@ class Engine:
                      recount_percent: int = 50, peel_blocks: int = 0) -> None:
         s = Schedule(support_group, chunk_width, compact_percent, recount_percent, peel_blocks)
         _check(lib().kt_engine_set_schedule(self._h, ctypes.byref(s)))
+
+    def set_wait_limit(self, base_ns: int, ns_per_unit: int = 8) -> None:
+        """Bound of every peel barrier wait: base_ns plus ns_per_unit per unit of covered work."""
+        _check(lib().kt_engine_set_wait_limit(self._h, base_ns, ns_per_unit))
+
+    def wait_limit(self) -> tuple:
+        b, u = ctypes.c_uint64(0), ctypes.c_uint32(0)
+        _check(lib().kt_engine_get_wait_limit(self._h, ctypes.byref(b), ctypes.byref(u)))
+        return b.value, u.value
 
     def schedule(self) -> Schedule:
         s = Schedule()

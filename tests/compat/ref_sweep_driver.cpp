@@ -2,8 +2,11 @@
 // (kernel.h:12), compiled from its unmodified sources, over many configurations of one graph that is
 // read once with the reference's own reader (createCOOFromFile, graph.cu:37-79).  Configurations
 // are command lines of the reference CLI, parsed by its own parseArgs (config.h:183-224), one per
-// line on standard input.  A line starting with "chain" instead decomposes the graph by chaining
-// single-k runs k = 3, 4, ... (each on the previous output) with the options that follow.
+// line on standard input.  A line "chain <K> <options>" instead decomposes the graph by chaining
+// single-k runs k = 3, 4, ..., K (each on the previous output) with the options that follow.  K is
+// the graph's k_max: the reference's GPU path cannot run the level after it, whose k-truss is
+// empty (with no edge left, removeCOOCSRDeletedEdgesOnDevice launches histogram_kernel with zero
+// blocks, graph.cu:520-525, and the thrust scan that follows aborts on that launch error).
 //
 // Output per run (the reference prints its own "<CSV config>, <ms> ms" lines with -v 0):
 //   RESULT k=<k> edges=<undirected truss edges> hash=<order-free hash of the edge set>
@@ -85,7 +88,16 @@ int main(int argc, char** argv) {
         while (!line.empty() && (line.back() == '\n' || line.back() == '\r')) line.pop_back();
         if (line.empty()) continue;
         const bool chain = line.compare(0, 5, "chain") == 0;
-        Config c = parse_line(chain ? line.substr(5) : line, argv[1]);
+        unsigned last_k = 0;
+        std::string opts = line;
+        if (chain) {
+            opts = line.substr(5);
+            size_t i = opts.find_first_not_of(' ');
+            last_k = (unsigned)std::strtoul(opts.c_str() + (i == std::string::npos ? 0 : i), nullptr, 10);
+            i = opts.find(' ', i == std::string::npos ? 0 : i);
+            opts = i == std::string::npos ? std::string() : opts.substr(i);
+        }
+        Config c = parse_line(opts, argv[1]);
         if (!chain) {
             COOGraph* g = copy_of(graph);  // ktruss relabels its input in place (kernel.cu:18)
             COOGraph* t = createEmptyCOO(g->numNodes, g->numEdges ? g->numEdges : 1);
@@ -102,7 +114,7 @@ int main(int argc, char** argv) {
             continue;
         }
         COOGraph* cur = copy_of(graph);
-        for (unsigned k = 3; cur->numEdges > 0; ++k) {
+        for (unsigned k = 3; cur->numEdges > 0 && k <= last_k; ++k) {
             COOGraph* in = copy_of(cur);
             COOGraph* t = createEmptyCOO(in->numNodes, in->numEdges);
             Config ck = c;

@@ -177,6 +177,33 @@ def test_barrier_wait_is_bounded_and_engine_recovers():
     eng.close()
 
 
+def test_long_rounds_fit_their_work_scaled_wait_limit():
+    """A base wait limit of 1 ms, far below the longest round of this query: every barrier's limit
+    also grows with the work it covers (row entries queued for the round), so the query completes
+    and matches the oracle instead of timing out."""
+    torch = pytest.importorskip("torch")
+    n, u, v = kt.gen_rmat(18, 16, 0.57, 0.19, 0.19, 3)
+    src, dst = both_directions(u, v)
+    eng = kt.Engine(0)
+    assert eng.wait_limit() == (10_000_000_000, 8)
+    with pytest.raises(kt.KtrussError):
+        eng.set_wait_limit(10)  # below 1 microsecond
+    eng.set_wait_limit(1_000_000, 8)
+    eng.set_schedule(8, 32, 85, 0)  # no recount: the first round walks the rows of most edges
+    d_src = torch.from_numpy(src.view(np.int32)).cuda()
+    d_dst = torch.from_numpy(dst.view(np.int32)).cuda()
+    d_keep = torch.zeros(len(src), dtype=torch.uint8, device="cuda")
+    torch.cuda.synchronize()
+    k = 60
+    eng.ktruss(d_src.data_ptr(), d_dst.data_ptr(), len(src), n, k, d_keep.data_ptr())
+    log = eng.round_log()
+    assert int(np.asarray(log["ns"]).max()) > 1_000_000, "no round longer than the base limit: test is vacuous"
+    keep = d_keep.cpu().numpy().astype(bool)
+    os_, od = oracle.ktruss(n, src, dst, k)
+    assert np.array_equal(edge_keys(src[keep], dst[keep]), edge_keys(os_, od))
+    eng.close()
+
+
 @pytest.mark.parametrize("k", [2, 3, 5, 9])
 def test_engine_single_k_keep_mask(k):
     torch = pytest.importorskip("torch")

@@ -17,8 +17,8 @@ GRAPHS = [
     ("ws8000", lambda: kt.gen_ws(8000, 10, 0.1, 14)),
 ]
 
-SCHEDULES = list(itertools.product((4, 8, 16, 32), (8, 16, 32), (0, 50, 85), (0, 1, 50), (0,))) + \
-    list(itertools.product((8,), (8, 32), (0, 85), (0, 50), (1, 2)))
+SCHEDULES = list(itertools.product((0, 4, 8, 16, 32), (8, 16, 32), (0, 50, 85), (0, 1, 50), (0,))) + \
+    list(itertools.product((0, 8), (8, 32), (0, 85), (0, 50), (1, 2)))
 
 
 @pytest.fixture(scope="module")
@@ -128,3 +128,33 @@ def test_chunk_buffer_overflow(sizes, w, rc, pb, torch):
     out = d_out.cpu().numpy().view(np.uint32)
     assert int(d_k.item()) == max(sizes)
     assert np.array_equal(out[:m], expect) and np.array_equal(out[m:], expect)
+
+
+def test_vertex_hash_count_on_rows_beyond_its_tables(torch):
+    """The vertex-centric count (support group 0) on a 2,100-vertex clique with a pendant path: rows
+    of up to 2,099 oriented entries exceed the 2,048 of a block table (searched in HBM instead), the
+    top vertices have more in-edges than one block item takes (several items per vertex), and the
+    path's vertices go to single warps.  Clique edges have truss number 2,100, path edges 2."""
+    s_ = 2100
+    iu, iv = np.triu_indices(s_, 1)
+    path_u = np.arange(s_ - 1, s_ + 40, dtype=np.int64)
+    u = np.concatenate([iu, path_u]).astype(np.uint32)
+    v = np.concatenate([iv, path_u + 1]).astype(np.uint32)
+    n = s_ + 41
+    src, dst = both_directions(u, v)
+    eng = kt.Engine(0)
+    d_src = torch.from_numpy(src.view(np.int32)).cuda()
+    d_dst = torch.from_numpy(dst.view(np.int32)).cuda()
+    d_out = torch.empty(len(src), dtype=torch.int32, device="cuda")
+    d_k = torch.zeros(1, dtype=torch.int32, device="cuda")
+    want = np.where(np.arange(len(u)) < len(iu), s_, 2).astype(np.uint32)
+    for g in (0, 8):
+        eng.set_schedule(g, 32, 85, 50, 0)
+        d_out.fill_(-1)
+        torch.cuda.synchronize()
+        eng.decompose(d_src.data_ptr(), d_dst.data_ptr(), len(src), n, d_out.data_ptr(), d_k.data_ptr())
+        out = d_out.cpu().numpy().view(np.uint32)
+        assert int(d_k.item()) == s_, g
+        assert np.array_equal(out[: len(u)], want) and np.array_equal(out[len(u):], want), g
+        assert eng.stats().triangles == s_ * (s_ - 1) * (s_ - 2) // 6, g
+    eng.close()
