@@ -145,6 +145,52 @@ def load_er4096():
     return man["num_nodes"], np.concatenate([u, v]), np.concatenate([v, u]), t, man["k_max"]
 
 
+def gpu_local_cpus(index):
+    """CPUs of the GPU's own NUMA node (sysfs local_cpulist of its PCI device), or None."""
+    try:
+        bus = subprocess.run(["nvidia-smi", f"--id={index}", "--query-gpu=pci.bus_id", "--format=csv,noheader"],
+                             capture_output=True, text=True, timeout=30).stdout.strip().lower()
+        dom, rest = bus.split(":", 1)
+        base = f"/sys/bus/pci/devices/{dom[-4:]}:{rest}"
+        with open(os.path.join(base, "local_cpulist")) as f:
+            text = f.read().strip()
+        node = None
+        try:
+            with open(os.path.join(base, "numa_node")) as f:
+                node = int(f.read().strip())
+        except Exception:
+            pass
+        cpus = set()
+        for part in text.split(","):
+            if "-" in part:
+                a, b = part.split("-")
+                cpus.update(range(int(a), int(b) + 1))
+            elif part:
+                cpus.add(int(part))
+        return {"cpus": sorted(cpus), "numa_node": node, "cpulist": text}
+    except Exception:
+        return None
+
+
+def bind_near_gpu(index):
+    """Runs the calling thread (and the pinned host buffers it allocates, placed on first touch) on
+    the GPU's own NUMA node, so that host<->device copies do not cross sockets.  Returns a record
+    of what was done."""
+    info = gpu_local_cpus(index)
+    if not info or not info["cpus"]:
+        return {"bound": False, "why": "no local CPU list for the GPU"}
+    try:
+        avail = os.sched_getaffinity(0)
+        cpus = [c for c in info["cpus"] if c in avail]
+        if not cpus or len(cpus) == len(avail):
+            return {"bound": False, "numa_node": info["numa_node"], "cpulist": info["cpulist"],
+                    "why": "the GPU's CPUs are all this process's CPUs"}
+        os.sched_setaffinity(0, cpus)
+        return {"bound": True, "numa_node": info["numa_node"], "cpulist": info["cpulist"], "cpus": len(cpus)}
+    except Exception as exc:
+        return {"bound": False, "why": str(exc)}
+
+
 def host_threads():
     try:
         return len(os.sched_getaffinity(0))
@@ -482,6 +528,9 @@ def run_batch(args, world, rank, local):
     if not np.array_equal(k2, kmax.view(np.uint32)):
         raise RuntimeError("host-buffer and device-buffer batches differ")
     single = single_graph_path(kt, torch, eng, n, u, v, off, kmax.view(np.uint32), args.single_graphs)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu = batch_cpu_baseline(u, v, off, h_out, kmax.view(np.uint32))
     line = {"metric": "batched k-truss decomposition graphs/s", "value": G * world / (ms * 1e-3),
             "unit": "graphs/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
@@ -499,11 +548,41 @@ def run_batch(args, world, rank, local):
                     "last_call_device_ms": {"copy_in": ls.copy_in_ms, "decompose": ls.last_ms,
                                             "copy_out_and_kmax": ls.copy_out_ms}},
             "gpu_launches": launches, "clocks": clk.summary()}
+    if cpu:
+        line["cpu_baseline"], line["detail_parity"] = cpu
     if rank == 0:
         print(json.dumps(line), flush=True)
     eng.close()
     if dist:
         td.destroy_process_group()
+
+
+def batch_cpu_baseline(u, v, off, truss, kmax):
+    """The reference algorithm on the host cores for the whole batch: every graph decomposed by
+    chained single-k runs (the oracle port of kernel_hdc.cu), one single-threaded process per graph
+    at a time on all host cores; each graph's k_max and truss numbers (sha256) are compared with the
+    GPU's batch output."""
+    import hashlib
+
+    oracle = oracle_module()
+    res, secs, workers = oracle.decompose_batch_processes(u, v, off)
+    G = len(off) - 1
+    lo = np.searchsorted(u, off[:-1], side="left")
+    hi = np.searchsorted(u, off[1:], side="left")
+    bad = 0
+    for g, k_ref, sha_ref in res:
+        got = hashlib.sha256(np.ascontiguousarray(truss[lo[g]:hi[g]]).astype("<u4").tobytes()).hexdigest()
+        if got != sha_ref or int(kmax[g]) != k_ref:
+            bad += 1
+    if len(res) != G or bad:
+        raise RuntimeError(f"batch: {bad} of {G} graphs differ from the reference algorithm on the CPU")
+    base = {"value": G / secs, "unit": "graphs/s", "cores": workers, "kind": "port",
+            "sample": f"all {G} graphs of the batch, each decomposed completely by the reference algorithm "
+                      "(chained count-and-prune single-k runs, the oracle port of kernel_hdc.cu), one "
+                      f"single-threaded process per graph at a time on {workers} host processes ({secs:.1f} s)"}
+    parity = (f"all {G} graphs: per-edge truss numbers (sha256) and k_max equal the reference algorithm's "
+              "(CPU chain)")
+    return base, parity
 
 
 def single_graph_path(kt, torch, eng, n, u, v, off, kmax, count):
@@ -814,10 +893,15 @@ def run_ours(args, world, rank, local):
     if int(d_k.item()) != ek or not np.array_equal(d_eo.cpu().numpy().view(np.uint32)[: len(et)], et):
         raise RuntimeError("er4096 decomposition differs from its fixture")
 
-    # end to end through the host-buffer C ABI (pinned host memory)
+    # end to end through the host-buffer C ABI (pinned host memory placed on the GPU's NUMA node:
+    # allocated and first touched from its CPUs; the thread's CPU set is restored afterwards)
+    cpus0 = os.sched_getaffinity(0)
+    numa = bind_near_gpu(local)
     h_src = torch.from_numpy(src.view(np.int32)).pin_memory()
     h_dst = torch.from_numpy(dst.view(np.int32)).pin_memory()
     h_out = torch.empty(N, dtype=torch.int32).pin_memory()
+    h_out.fill_(0)
+    os.sched_setaffinity(0, cpus0)
     g = kt.COOGraph(n, h_src.numpy().view(np.uint32), h_dst.numpy().view(np.uint32))
     out_np = h_out.numpy().view(np.uint32)
     kt.decompose(g, out=out_np)
@@ -873,7 +957,10 @@ def run_ours(args, world, rank, local):
             "e2e": {"value": replica_throughput(m, world, e2e_s * 1e3), "unit": "edges/s", "h2d_bytes_per_step": 8 * N,
                     "d2h_bytes_per_step": 4 * N, "ms_per_step": e2e_s * 1e3,
                     "last_call_device_ms": {"copy_in": ls.copy_in_ms, "decompose": ls.last_ms,
-                                            "copy_out": ls.copy_out_ms}},
+                                            "copy_out": ls.copy_out_ms},
+                    "h2d_gbs": 8 * N / (ls.copy_in_ms * 1e-3) / 1e9 if ls.copy_in_ms else None,
+                    "d2h_gbs": 4 * N / (ls.copy_out_ms * 1e-3) / 1e9 if ls.copy_out_ms else None,
+                    "host_buffers": numa},
             "gpu_launches": launches,
             "roofline": {"bound": "hbm", "kernel": "k_peel", "achieved": pk_gbs, "peak": hbm,
                          "peak_kind": hbm_kind, "unit": "GB/s", "frac": pk_gbs / hbm,

@@ -223,6 +223,29 @@ int kt_engine_reserve(kt_engine* engine, uint32_t max_nodes, uint64_t max_entrie
 int kt_engine_decompose(kt_engine* engine, const uint32_t* d_src, const uint32_t* d_dst,
                         uint64_t num_entries, uint32_t num_nodes, uint32_t* d_truss_per_entry,
                         uint32_t* d_k_max, int sync);
+/* The reference's variant switches for single-k truss calls (config.h:51-161; -d, -f, -r, -b, -t,
+ * -y): every variant gives the same k-truss.  directedness KT_DIRECTED_BY_DEGREE (default) or
+ * KT_DIRECTED_BY_INDEX orients edges from lower to higher degree rank or vertex id and runs the
+ * engine's peel; recount KT_RECOUNT_ALL lets rounds that remove a large share of the edges recount
+ * all survivors (the schedule's recount_percent), KT_RECOUNT_AFFECTED updates only the triangles
+ * of removed edges (support decrements in every round).  KT_UNDIRECTED runs count-and-delete
+ * passes over the symmetric rows with counts capped at k-2 (the reference's undirected variant;
+ * with KT_RECOUNT_AFFECTED a pass recounts only edges next to the previous pass's deletions).
+ * input_format KT_FORMAT_TILED_COOCSR counts support over the tiled COO/CSR layout (num_tiles x
+ * num_tiles tiles, num_parallel_tiles column tiles of one edge processed in parallel) in recount
+ * passes.  block_size: threads per block of the variant passes' kernels (the reference's -b). */
+typedef struct kt_variant {
+    int32_t directedness;
+    int32_t input_format;
+    int32_t recount;
+    uint32_t block_size;
+    uint32_t num_tiles;
+    uint32_t num_parallel_tiles;
+} kt_variant;
+kt_variant kt_variant_default(void);
+/* The variant of the engine's later kt_engine_ktruss calls (decompositions ignore it). */
+int kt_engine_set_variant(kt_engine* engine, const kt_variant* variant);
+int kt_engine_get_variant(kt_engine* engine, kt_variant* variant);
 /* Device-resident single-k truss: d_keep[i] = 1 if entry i's edge is in the k-truss, else 0. */
 int kt_engine_ktruss(kt_engine* engine, const uint32_t* d_src, const uint32_t* d_dst,
                      uint64_t num_entries, uint32_t num_nodes, uint32_t k, uint8_t* d_keep,

@@ -30,7 +30,7 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompil
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-unused-function"]
 
 LIB_SOURCES = ["kt_host.cpp", "kt_gen.cpp", "kt_sort.cu", "kt_build.cu", "kt_support.cu", "kt_peel.cu",
-               "kt_engine.cu", "kt_noalloc.cu", "kt_selector.cu", "kt_ingest.cu"]
+               "kt_engine.cu", "kt_noalloc.cu", "kt_selector.cu", "kt_ingest.cu", "kt_variants.cu"]
 CLI_SOURCES = ["ktruss_cli.cpp"]
 COMPAT_SOURCES = ["ktruss_compat.cpp"]
 

@@ -60,6 +60,19 @@ __global__ void k_rank_keys(const uint32_t* __restrict__ deg, uint32_t n, unsign
     if (v < n) keys[v] = ((uint64_t)deg[v] << vb) | v;
 }
 
+// Orientation by vertex id (KT_DIRECTED_BY_INDEX, graph.cu:194-207 without the relabel of
+// kernel.cu:13-20): rank[v] = v; row_len[v] = degree.
+__global__ void k_rank_identity(const uint32_t* __restrict__ deg, uint32_t n, uint32_t* __restrict__ rank,
+                                uint32_t* __restrict__ row_len) {
+    uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v < n) {
+        rank[v] = v;
+        row_len[v] = deg[v];
+    } else if (v == n) {
+        row_len[n] = 0;
+    }
+}
+
 // rank[v] = sorted position; row_len[rank] = degree (row lengths of the symmetric CSR).
 __global__ void k_rank_scatter(const uint64_t* __restrict__ sorted, uint32_t n, unsigned vb,
                                uint32_t* __restrict__ rank, uint32_t* __restrict__ row_len) {
@@ -433,16 +446,23 @@ int build_graph(kt_engine* e, const uint32_t* d_src, const uint32_t* d_dst, uint
     // (input errors are read back once, at the end of the build: every kernel before that
     // check indexes inside its arrays whatever the input)
 
-    // 2. ranks: ascending (degree, id)
-    k_rank_keys<<<grid_for(n), kThreads, 0, st>>>(e->deg, n, vb, e->key_a);
-    count_launch(e);
-    if ((rc = check_launch(e, "k_rank_keys"))) return rc;
+    // 2. ranks: ascending (degree, id), or the ids themselves when orienting by index
     int in_b = 0;
-    if ((rc = radix_sort(e, e->key_a, nullptr, e->key_b, nullptr, n, vb + bits_for(entries + 2), &in_b))) return rc;
-    k_rank_scatter<<<grid_for((uint64_t)n + 1), kThreads, 0, st>>>(in_b ? e->key_b : e->key_a, n, vb, e->rank,
-                                                                   e->s_len);
-    count_launch(e);
-    if ((rc = check_launch(e, "k_rank_scatter"))) return rc;
+    if (e->orient_by_index) {
+        k_rank_identity<<<grid_for((uint64_t)n + 1), kThreads, 0, st>>>(e->deg, n, e->rank, e->s_len);
+        count_launch(e);
+        if ((rc = check_launch(e, "k_rank_identity"))) return rc;
+    } else {
+        k_rank_keys<<<grid_for(n), kThreads, 0, st>>>(e->deg, n, vb, e->key_a);
+        count_launch(e);
+        if ((rc = check_launch(e, "k_rank_keys"))) return rc;
+        if ((rc = radix_sort(e, e->key_a, nullptr, e->key_b, nullptr, n, vb + bits_for(entries + 2), &in_b)))
+            return rc;
+        k_rank_scatter<<<grid_for((uint64_t)n + 1), kThreads, 0, st>>>(in_b ? e->key_b : e->key_a, n, vb, e->rank,
+                                                                       e->s_len);
+        count_launch(e);
+        if ((rc = check_launch(e, "k_rank_scatter"))) return rc;
+    }
     // row starts of the symmetric CSR (row r holds the neighbours of the rank-r vertex)
     if ((rc = exclusive_scan(e, e->s_len, e->s_ptr, (uint64_t)n + 1))) return rc;
 

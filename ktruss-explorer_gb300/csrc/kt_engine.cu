@@ -230,18 +230,41 @@ int run_decompose(kt_engine* e, const uint32_t* d_src, const uint32_t* d_dst, ui
     return fill_graph_stats(e);
 }
 
+// The single-k pipeline after the build, by the engine's variant: the engine's peel (oriented by
+// degree or by index; recount all = the schedule's recount rounds, affected = decrements only), or
+// count-and-delete passes (undirected capped counts; tiled counts).
+int single_k_body(kt_engine* e, uint32_t k) {
+    int rc;
+    const kt_variant& v = e->variant;
+    if (v.input_format == KT_FORMAT_TILED_COOCSR) return kt::ktruss_tiled(e, k, v.recount == KT_RECOUNT_ALL,
+                                                                        v.directedness == KT_UNDIRECTED);
+    if (v.directedness == KT_UNDIRECTED) return kt::ktruss_undirected(e, k, v.recount == KT_RECOUNT_ALL, 8);
+    if (k >= 3 && (rc = kt::count_support(e))) return rc;
+    if (!e->trusted && (rc = record(e, e->ev_counted))) return rc;
+    const uint32_t saved = e->sched.recount_percent;
+    if (v.recount == KT_RECOUNT_AFFECTED) e->sched.recount_percent = 0;
+    rc = kt::peel_single_k(e, k);
+    e->sched.recount_percent = saved;
+    return rc;
+}
+
+// Whether the variant's single-k pipeline runs without host reads after the build (capturable).
+bool single_k_capturable(const kt_engine* e) {
+    return e->variant.input_format != KT_FORMAT_TILED_COOCSR && e->variant.directedness != KT_UNDIRECTED;
+}
+
 int run_ktruss(kt_engine* e, const uint32_t* d_src, const uint32_t* d_dst, uint64_t entries, uint32_t n, uint32_t k,
                uint8_t* d_keep) {
     int rc;
     if ((rc = record_start(e))) return rc;
-    if ((rc = kt::build_graph(e, d_src, d_dst, entries, n))) return rc;
+    e->orient_by_index = e->variant.directedness == KT_DIRECTED_BY_INDEX;
+    rc = kt::build_graph(e, d_src, d_dst, entries, n);
+    e->orient_by_index = false;
+    if (rc) return rc;
     if ((rc = record(e, e->ev_select))) return rc;
     if ((rc = record(e, e->ev_built))) return rc;
-    if (k >= 3) {
-        if ((rc = kt::count_support(e))) return rc;
-    }
-    if ((rc = record(e, e->ev_counted))) return rc;
-    if ((rc = kt::peel_single_k(e, k))) return rc;
+    if ((rc = single_k_body(e, k))) return rc;
+    if (!single_k_capturable(e) && (rc = record(e, e->ev_counted))) return rc;
     if ((rc = kt::emit_keep(e, d_keep))) return rc;
     if ((rc = record_stop(e))) return rc;
     return fill_graph_stats(e);
@@ -254,14 +277,16 @@ int replay_pipeline(kt_engine* e) {
     e->big_row = c.big_row;  // other calls since may have built other graphs
     e->tiny_row = c.tiny_row;
     int rc;
-    if ((rc = kt::build_graph(e, c.src, c.dst, c.entries, c.n))) return rc;
+    if (c.kind == 1 && (rc = kt::build_graph(e, c.src, c.dst, c.entries, c.n))) return rc;
     if (c.kind == 1)
         return (rc = kt::count_support(e)) || (rc = kt::peel_decompose(e)) ||
                        (rc = kt::emit_truss_per_entry(e, c.truss, c.k_max))
                    ? rc
                    : KT_OK;
-    if (c.k >= 3 && (rc = kt::count_support(e))) return rc;
-    if ((rc = kt::peel_single_k(e, c.k)) || (rc = kt::emit_keep(e, c.keep))) return rc;
+    e->orient_by_index = e->variant.directedness == KT_DIRECTED_BY_INDEX;
+    rc = kt::build_graph(e, c.src, c.dst, c.entries, c.n);
+    e->orient_by_index = false;
+    if (rc || (rc = single_k_body(e, c.k)) || (rc = kt::emit_keep(e, c.keep))) return rc;
     return KT_OK;
 }
 
@@ -270,6 +295,8 @@ int replay_pipeline(kt_engine* e) {
 int replay(kt_engine* e, int sync) {
     if (!e->last.kind) return fail(KT_ERR_INVALID_ARG, "kt_engine_replay: no decomposition or single-k call to repeat");
     int rc;
+    if (!e->replay && !e->replay_direct && e->last.kind == 2 && !single_k_capturable(e))
+        e->replay_direct = true;  // variant passes read a flag per pass: launched directly
     if (!e->replay && !e->replay_direct) {
         const uint64_t l0 = e->launches;
         cudaGraph_t g = nullptr;
@@ -365,6 +392,7 @@ int kt_engine_destroy(kt_engine* e) {
     kt::drop_replay(e);
     if (e->arena) cudaFree(e->arena);
     if (e->aux) cudaFree(e->aux);
+    if (e->tile_off) cudaFree(e->tile_off);
     if (e->ctrl) cudaFree(e->ctrl);
     if (e->h_ctrl) cudaFreeHost(e->h_ctrl);
     if (e->ev_start) cudaEventDestroy(e->ev_start);
@@ -442,6 +470,33 @@ int kt_engine_replay(kt_engine* e, int sync) {
 int kt_engine_replay_mode(const kt_engine* e) { return !e ? 0 : e->replay ? 1 : e->replay_direct ? 2 : 0; }
 
 kt_schedule kt_schedule_default(void) { return kt_schedule{8, 32, 85, 50, 0}; }
+
+kt_variant kt_variant_default(void) {
+    return kt_variant{KT_DIRECTED_BY_DEGREE, KT_FORMAT_COOCSR, KT_RECOUNT_ALL, 512, 8, 8};
+}
+
+int kt_engine_set_variant(kt_engine* e, const kt_variant* v) {
+    kt::clear_error();
+    if (!e || !v) return fail(KT_ERR_INVALID_ARG, "kt_engine_set_variant: null argument");
+    if (v->directedness < KT_UNDIRECTED || v->directedness > KT_DIRECTED_BY_DEGREE ||
+        v->input_format < KT_FORMAT_COOCSR || v->input_format > KT_FORMAT_TILED_COOCSR ||
+        v->recount < KT_RECOUNT_ALL || v->recount > KT_RECOUNT_AFFECTED)
+        return fail(KT_ERR_INVALID_ARG, "kt_engine_set_variant: bad enum value");
+    if (v->block_size < 1 || v->block_size > 1024)
+        return fail(KT_ERR_INVALID_ARG, "block_size must be 1..1024 (got %u)", v->block_size);
+    if (v->num_tiles < 1 || v->num_tiles > 4096 || v->num_parallel_tiles < 1)
+        return fail(KT_ERR_INVALID_ARG, "num_tiles must be 1..4096 and num_parallel_tiles >= 1");
+    e->variant = *v;
+    kt::drop_replay(e);
+    return KT_OK;
+}
+
+int kt_engine_get_variant(kt_engine* e, kt_variant* v) {
+    kt::clear_error();
+    if (!e || !v) return fail(KT_ERR_INVALID_ARG, "kt_engine_get_variant: null argument");
+    *v = e->variant;
+    return KT_OK;
+}
 
 int kt_engine_set_schedule(kt_engine* e, const kt_schedule* s) {
     kt::clear_error();
@@ -727,6 +782,7 @@ int kt_decompose_batch(const uint32_t* src, const uint32_t* dst, uint64_t num_en
     const size_t need = 2 * (size_t)num_graphs + 1;
     if (e->aux_words < need) {
         if (e->aux) cudaFree(e->aux);
+    if (e->tile_off) cudaFree(e->tile_off);
         e->aux = nullptr;
         e->aux_words = 0;
         if ((rc = check_cuda(cudaMalloc(&e->aux, sizeof(uint32_t) * need), "allocate batch staging"))) return rc;
@@ -810,6 +866,12 @@ int kt_ktruss(const kt_coo* graph, kt_coo* truss, const kt_config* config) {
     std::lock_guard<std::mutex> lock(g_default_mu);
     kt::forget(e);  // host-buffer calls overwrite the staging buffers a replay would read
     if ((rc = check_cuda(cudaSetDevice(e->device), "cudaSetDevice"))) return rc;
+    // the reference's variant switches select the single-k path (-d, -f, -r, -b, -t, -y)
+    const kt_variant variant{config->directedness, config->input_format, config->recount,
+                             config->block_size ? config->block_size : 512u,
+                             config->num_tiles ? config->num_tiles : 8u,
+                             config->num_parallel_tiles ? config->num_parallel_tiles : 8u};
+    if ((rc = kt_engine_set_variant(e, &variant))) return rc;
     const uint64_t N = graph->num_edges;
     const int verbose = config->verbosity >= 1;
     double t0 = now_ms();

@@ -81,6 +81,8 @@ struct kt_engine {
     uint8_t* out_u8 = nullptr;
     uint32_t* aux = nullptr;       // batch staging: vertex offsets and per-graph k_max (own allocation)
     size_t aux_words = 0;
+    uint32_t* tile_off = nullptr;  // tiled variant: first oriented position of each (vertex, column tile)
+    size_t tile_off_words = 0;     //   (own allocation, made by the first tiled call)
 
     // Current graph.
     uint32_t n = 0;
@@ -89,6 +91,9 @@ struct kt_engine {
     uint32_t vb = 1;  // bits per rank in sort keys
 
     kt_schedule sched{8, 32, 85, 50, 0};  // kernel schedule (kt_engine_set_schedule)
+    kt_variant variant{KT_DIRECTED_BY_DEGREE, KT_FORMAT_COOCSR, KT_RECOUNT_ALL, 512, 8, 8};  // single-k calls
+    bool orient_by_index = false;      // the current build orients by vertex id (KT_DIRECTED_BY_INDEX)
+    uint32_t variant_passes = 0;       // passes of the last undirected or tiled single-k call
     uint64_t wait_base_ns = 10ull * 1000 * 1000 * 1000;  // peel barrier wait limit: base ...
     uint64_t wait_ns_per_unit = 8;                        // ... plus per unit of covered work
     bool batch_call = false;           // the current call decomposes a batch of separate graphs
@@ -97,7 +102,7 @@ struct kt_engine {
     float* sel_feat = nullptr;         // the 16 features
     uint32_t* sel_choice = nullptr;    // the selector's schedule index
     kt_stats stats{};
-    int peel_mode = 0;          // 0 decomposition, 1 single-k
+    int peel_mode = 0;          // 0 decomposition, 1 single-k peel, 2 k < 3, 3 single-k variant passes
     // Replay (kt_engine_replay): the last decomposition or single-k call on device buffers, and
     // its device pipeline as an instantiated CUDA graph once captured.  `trusted` marks a pipeline
     // run whose input already passed its checks: no host reads, no timing events (capturable).
@@ -175,5 +180,9 @@ int select_schedule(kt_engine* e);
 int finish_stats(kt_engine* e);
 // Launches a grid barrier that cannot complete and returns the status it reports.
 int barrier_timeout_probe(kt_engine* e, uint64_t timeout_ns);
+// kt_variants.cu: single-k truss by count-and-delete passes (undirected capped counts; tiled
+// counts); edge states in e->rnd, so emit_keep applies.  Synchronous (one read per pass).
+int ktruss_undirected(kt_engine* e, uint32_t k, bool recount_all, uint32_t group);
+int ktruss_tiled(kt_engine* e, uint32_t k, bool recount_all, bool capped);
 
 }  // namespace kt

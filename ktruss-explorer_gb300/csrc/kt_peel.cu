@@ -901,13 +901,14 @@ int finish_stats(kt_engine* e) {
         int rc = check_cuda(cudaEventElapsedTime(&e->stats.last_ms, e->ev_start, e->ev_stop), "elapsed time");
         if (rc) return rc;
     }
-    if (e->m == 0 || e->peel_mode == 2) {
+    if (e->m == 0 || e->peel_mode == 2 || e->peel_mode == 3) {
         e->stats.compactions = 0;
         e->stats.walk_entries = 0;
         e->stats.peel_kernel_ms = 0;
         for (int i = 0; i < 6; ++i) e->stats.peel_phase_ms[i] = 0;
         e->stats.k_max = 0;
         e->stats.num_rounds = e->stats.num_levels = e->stats.plain_passes = 0;
+        if (e->m && e->peel_mode == 3) e->stats.num_rounds = e->variant_passes;  // count-and-delete passes
         e->stats.plain_alive_sum = 0;
         e->stats.triangles = 0;
         e->stats_ready = true;

@@ -79,6 +79,14 @@ class Stats(ctypes.Structure):
         return d
 
 
+class Variant(ctypes.Structure):
+    """kt_variant: the reference's -d/-f/-r/-b/-t/-y switches for single-k truss calls (every
+    variant gives the same k-truss; they select different kernel paths)."""
+    _fields_ = [("directedness", ctypes.c_int32), ("input_format", ctypes.c_int32), ("recount", ctypes.c_int32),
+                ("block_size", ctypes.c_uint32), ("num_tiles", ctypes.c_uint32),
+                ("num_parallel_tiles", ctypes.c_uint32)]
+
+
 class Schedule(ctypes.Structure):
     """kt_schedule: lanes per edge of the support count, row entries per peel chunk, the
     alive-edge percentage below which rows are compacted (0 = never), and the frontier share of
@@ -147,6 +155,10 @@ def lib() -> ctypes.CDLL:
         L.kt_engine_round_log.argtypes = [_VP, _U32P, _U32P, _U32P, ctypes.c_uint32, _U32P]
         L.kt_schedule_default.restype = Schedule
         L.kt_schedule_default.argtypes = []
+        L.kt_variant_default.restype = Variant
+        L.kt_variant_default.argtypes = []
+        L.kt_engine_set_variant.argtypes = [_VP, ctypes.POINTER(Variant)]
+        L.kt_engine_get_variant.argtypes = [_VP, ctypes.POINTER(Variant)]
         L.kt_engine_set_schedule.argtypes = [_VP, ctypes.POINTER(Schedule)]
         L.kt_engine_get_schedule.argtypes = [_VP, ctypes.POINTER(Schedule)]
         L.kt_engine_set_wait_limit.argtypes = [_VP, ctypes.c_uint64, ctypes.c_uint32]
@@ -404,6 +416,19 @@ class Engine:
                      recount_percent: int = 50, peel_blocks: int = 0) -> None:
         s = Schedule(support_group, chunk_width, compact_percent, recount_percent, peel_blocks)
         _check(lib().kt_engine_set_schedule(self._h, ctypes.byref(s)))
+
+    def set_variant(self, directedness: str = "directed-by-degree", input_format: str = "coocsr",
+                    recount: str = "all", block_size: int = 512, num_tiles: int = 8,
+                    num_parallel_tiles: int = 8) -> None:
+        """Variant of later single-k calls, named as on the reference's command line."""
+        v = Variant(DIRECTEDNESS[directedness], INPUT_FORMAT[input_format], RECOUNT[recount], block_size, num_tiles,
+                    num_parallel_tiles)
+        _check(lib().kt_engine_set_variant(self._h, ctypes.byref(v)))
+
+    def variant(self) -> Variant:
+        v = Variant()
+        _check(lib().kt_engine_get_variant(self._h, ctypes.byref(v)))
+        return v
 
     def set_wait_limit(self, base_ns: int, ns_per_unit: int = 8) -> None:
         """Bound of every peel barrier wait: base_ns plus ns_per_unit per unit of covered work."""

@@ -162,6 +162,62 @@ def ktruss_runs(num_nodes: int, src, dst, k: int, runs: int, threads: int = 0):
     return os_[: num.value].copy(), od[: num.value].copy(), secs[:runs].copy(), passes[:runs].copy()
 
 
+def _batch_graph_job(args):
+    """Worker: decompose graphs [g0, g1) of a batch held in shared memory by the reference algorithm
+    (chained single-k runs) and return (graph, k_max, sha256 of its per-edge truss numbers)."""
+    import hashlib
+    from multiprocessing import shared_memory
+
+    names, M, G, g0, g1, method = args
+    shm = [shared_memory.SharedMemory(name=x) for x in names]
+    try:
+        u = np.ndarray((M,), np.uint32, buffer=shm[0].buf)
+        v = np.ndarray((M,), np.uint32, buffer=shm[1].buf)
+        off = np.ndarray((G + 1,), np.uint32, buffer=shm[2].buf)
+        lo = np.searchsorted(u, off[g0:g1], side="left")
+        hi = np.searchsorted(u, off[g0 + 1:g1 + 1], side="left")
+        out = []
+        for i, g in enumerate(range(g0, g1)):
+            a, b = int(lo[i]), int(hi[i])
+            lu, lv = u[a:b] - off[g], v[a:b] - off[g]
+            r = decompose(int(off[g + 1] - off[g]), np.concatenate([lu, lv]), np.concatenate([lv, lu]), method=method,
+                          threads=1)
+            out.append((g, r["k_max"], hashlib.sha256(r["truss"][: b - a].astype("<u4").tobytes()).hexdigest()))
+        return out
+    finally:
+        for x in shm:
+            x.close()
+
+
+def decompose_batch_processes(u, v, vertex_offsets, workers: int = 0, method: str = "chain", per_task: int = 8):
+    """Every graph of a batch (canonical edges u < v, graphs on consecutive vertex ranges) decomposed
+    by one single-threaded process per graph at a time, `workers` processes (spawned; the edges are
+    shared through shared memory).  Returns ([(graph, k_max, truss sha256)], seconds, workers)."""
+    import multiprocessing as mp
+    import time
+    from multiprocessing import shared_memory
+
+    workers = workers or (len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count())
+    arrays = [np.ascontiguousarray(u, np.uint32), np.ascontiguousarray(v, np.uint32),
+              np.ascontiguousarray(vertex_offsets, np.uint32)]
+    shm = [shared_memory.SharedMemory(create=True, size=max(a.nbytes, 1)) for a in arrays]
+    try:
+        for a, s_ in zip(arrays, shm):
+            np.ndarray(a.shape, a.dtype, buffer=s_.buf)[:] = a
+        G = len(arrays[2]) - 1
+        tasks = [([x.name for x in shm], len(arrays[0]), G, g, min(g + per_task, G), method)
+                 for g in range(0, G, per_task)]
+        t0 = time.perf_counter()
+        with mp.get_context("spawn").Pool(workers) as pool:
+            parts = pool.map(_batch_graph_job, tasks, chunksize=1)
+        secs = time.perf_counter() - t0
+    finally:
+        for x in shm:
+            x.close()
+            x.unlink()
+    return [r for part in parts for r in part], secs, workers
+
+
 def _peel_job(job):
     n, src, dst = job
     r = decompose(n, src, dst, method="peel", threads=1)

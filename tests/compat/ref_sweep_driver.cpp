@@ -6,7 +6,7 @@
 // single-k runs k = 3, 4, ..., K (each on the previous output) with the options that follow.  K is
 // the graph's k_max: the reference's GPU path cannot run the level after it, whose k-truss is
 // empty (with no edge left, removeCOOCSRDeletedEdgesOnDevice launches histogram_kernel with zero
-// blocks, graph.cu:520-525, and the thrust scan that follows aborts on that launch error).
+// blocks, graph.cu:541, and the thrust scan that follows aborts on that launch error).
 //
 // Output per run (the reference prints its own "<CSV config>, <ms> ms" lines with -v 0):
 //   RESULT k=<k> edges=<undirected truss edges> hash=<order-free hash of the edge set>
