@@ -392,8 +392,10 @@ int kt_selector_predict(kt_selector* selector, const float* features, uint32_t n
 int kt_engine_features(kt_engine* engine, const uint32_t* d_src, const uint32_t* d_dst, uint64_t num_entries,
                        uint32_t num_nodes, float* features);
 /* With a selector attached, every decomposition (single graph or batch) computes the features
- * of the built graph, runs the network on the device and uses its schedule (the call then waits
- * for the build before it enqueues the rest); NULL detaches it and keeps the last schedule. */
+ * of the built graph and runs the network on the device; the support count and the peel read the
+ * chosen schedule from device memory, so the call enqueues its whole pipeline without waiting
+ * (kt_engine_get_schedule and the statistics report the choice once the call has finished).  NULL
+ * detaches it; the engine keeps the last schedule it reported. */
 int kt_engine_set_selector(kt_engine* engine, kt_selector* selector);
 
 /* Self-test of the bounded device waits: launches a grid barrier that one block never reaches,

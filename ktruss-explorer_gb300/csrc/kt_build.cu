@@ -428,6 +428,7 @@ int build_graph(kt_engine* e, const uint32_t* d_src, const uint32_t* d_dst, uint
     e->n = n;
     e->entries = entries;
     e->m = (uint32_t)(entries / 2);
+    e->sched_on_device = false;  // a call with a selector sets it after the build
     e->vb = bits_for(n > 1 ? n : 2);
     const unsigned vb = e->vb;
     cudaStream_t st = e->stream;

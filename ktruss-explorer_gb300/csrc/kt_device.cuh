@@ -49,8 +49,22 @@ enum : uint32_t {
     kPChunks = 64,     // [4] u64 (words 64..71): work chunks claimed for the round; 64 bits
                        //     because a frontier of most edges can need more than 2^32 chunks
     kPWalk = 72,       // u64 (words 72..73): row entries queued for walks over the whole peel
+    kPSched = 76,      // [4] schedule chosen on the device by the learned selector: support group,
+                       //     chunk width, compaction and recount percentages (kept by the peel's init)
     kCtrlWords = 80,
 };
+
+// Schedule i of the autotuner's grid (kt_schedule_grid): support group {4, 8, 16} x chunk width
+// {8, 16, 32} x compaction {0, 85} x recount {0, 50}, the last varying fastest.  Shared by the host
+// grid and the selector's on-device choice.
+__host__ __device__ __forceinline__ void grid_schedule(uint32_t i, uint32_t* group, uint32_t* width,
+                                                       uint32_t* compact, uint32_t* recount) {
+    *recount = (i & 1u) ? 50u : 0u;
+    *compact = (i & 2u) ? 85u : 0u;
+    const uint32_t gw = i >> 2;  // group index * 3 + width index
+    *width = 8u << (gw % 3u);
+    *group = 4u << (gw / 3u);
+}
 
 __device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }
 

@@ -278,6 +278,7 @@ int replay_pipeline(kt_engine* e) {
     e->tiny_row = c.tiny_row;
     int rc;
     if (c.kind == 1 && (rc = kt::build_graph(e, c.src, c.dst, c.entries, c.n))) return rc;
+    if (c.kind == 1 && (rc = kt::select_schedule(e))) return rc;  // on the device: capturable
     if (c.kind == 1)
         return (rc = kt::count_support(e)) || (rc = kt::peel_decompose(e)) ||
                        (rc = kt::emit_truss_per_entry(e, c.truss, c.k_max))
@@ -567,16 +568,13 @@ int kt_get_schedule(kt_schedule* s) {
 }
 
 uint32_t kt_schedule_grid(kt_schedule* out, uint32_t cap) {
-    static const uint32_t groups[] = {4, 8, 16}, widths[] = {8, 16, 32}, compact[] = {0, 85}, recount[] = {0, 50};
-    uint32_t i = 0;
-    for (uint32_t g : groups)
-        for (uint32_t w : widths)
-            for (uint32_t c : compact)
-                for (uint32_t rc : recount) {
-                    if (out && i < cap) out[i] = kt_schedule{g, w, c, rc, 0};
-                    ++i;
-                }
-    return i;
+    const uint32_t count = KT_SELECTOR_SCHEDULES;  // 3 groups x 3 widths x 2 compactions x 2 recounts
+    for (uint32_t i = 0; out && i < count && i < cap; ++i) {
+        kt_schedule s{0, 0, 0, 0, 0};
+        kt::grid_schedule(i, &s.support_group, &s.chunk_width, &s.compact_percent, &s.recount_percent);
+        out[i] = s;
+    }
+    return count;
 }
 
 int kt_engine_autotune(kt_engine* e, const uint32_t* d_src, const uint32_t* d_dst, uint64_t num_entries,

@@ -98,6 +98,7 @@ struct kt_engine {
     uint64_t wait_ns_per_unit = 8;                        // ... plus per unit of covered work
     bool batch_call = false;           // the current call decomposes a batch of separate graphs
     kt_selector* selector = nullptr;   // learned schedule selector (kt_engine_set_selector)
+    bool sched_on_device = false;      // this call's schedule is the selector's choice in ctrl[kPSched]
     uint32_t* sel_stats = nullptr;     // 16 u64 graph statistics for the selector's features
     float* sel_feat = nullptr;         // the 16 features
     uint32_t* sel_choice = nullptr;    // the selector's schedule index
@@ -172,8 +173,9 @@ int emit_keep(kt_engine* e, uint8_t* d_keep);
 int emit_graph_kmax(kt_engine* e, const uint32_t* d_src, const uint32_t* d_dst, const uint32_t* d_offsets,
                     uint32_t num_graphs, const uint32_t* d_truss, uint32_t* d_kmax);
 // kt_selector.cu: graph statistics and features of the built graph into e->sel_feat (and, with
-// d_params, the selector's schedule index into e->sel_choice); select_schedule applies the
-// attached selector's choice to e->sched.
+// d_params, the selector's schedule index into e->sel_choice and that schedule into
+// ctrl[kPSched..]); select_schedule runs the attached selector on the device and marks the call's
+// schedule as device-chosen (e->sched_on_device; the support count and the peel read it there).
 int graph_features(kt_engine* e, const float* d_params);
 int select_schedule(kt_engine* e);
 // Reads the peel's control block and round log (stream must be drained); reports timeouts.

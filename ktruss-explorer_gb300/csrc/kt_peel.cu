@@ -92,11 +92,20 @@ struct PeelParams {
     uint32_t recount_num;  // a round whose frontier holds >= recount_num % of the alive edges
                            // recounts the survivors' support instead of decrementing (0: never)
     uint32_t single_k;  // 0: full decomposition; >= 3: the k of a single-k truss
+    const uint32_t* d_sched;  // non-null: chunk width, compaction and recount from these control
+                              // words (the selector's on-device choice) instead of the three above
     uint64_t wait_base_ns;      // wait limit of every grid barrier: base ...
     uint64_t wait_ns_per_unit;  // ... plus this per unit of work the wait covers
 };
 
 constexpr uint32_t kDead = 0xffffffffu;  // support of a removed edge
+
+// The launch's chunk width (log2), compaction and recount percentages, set once per block at the
+// start of k_peel from its parameters or from the device-side schedule choice.
+__shared__ uint32_t s_sched[3];
+__device__ __forceinline__ uint32_t cw_shift() { return s_sched[0]; }
+__device__ __forceinline__ uint32_t compact_num() { return s_sched[1]; }
+__device__ __forceinline__ uint32_t recount_num() { return s_sched[2]; }
 
 constexpr uint32_t kFirstChunk = 0x80000000u;
 constexpr uint32_t kNullChunk = 0xffffffffu;
@@ -124,7 +133,7 @@ __device__ __forceinline__ void push_edges(const PeelParams& P, uint32_t e, bool
             base = P.s_ptr[ux ? u : v];
             len = ux ? lu : lv;
         }
-        nch = len ? (len + (1u << P.cw_shift) - 1) >> P.cw_shift : 1;
+        nch = len ? (len + (1u << cw_shift()) - 1) >> cw_shift() : 1;
     }
     const uint32_t lane = lane_id(), slot = rr & 3;
     uint32_t incl = nch;
@@ -148,8 +157,8 @@ __device__ __forceinline__ void push_edges(const PeelParams& P, uint32_t e, bool
         if (take) {
             const uint32_t c0 = (uint32_t)cb + incl - nch;
             for (uint32_t c = 0; c < nch; ++c) {
-                const uint32_t off = c << P.cw_shift;
-                const uint32_t cnt = len > off ? min(1u << P.cw_shift, len - off) : 0u;
+                const uint32_t off = c << cw_shift();
+                const uint32_t cnt = len > off ? min(1u << cw_shift(), len - off) : 0u;
                 ch[c0 + c] = make_uint4(e, y, base + off, cnt | (c == 0 ? kFirstChunk : 0u));
             }
         }
@@ -407,6 +416,19 @@ template <int kBlocksPerSm>
 __global__ void __launch_bounds__(kPeelThreads, kBlocksPerSm) k_peel(PeelParams P) {
     __shared__ uint32_t warp_cnt[kPeelThreads / 32];
     uint32_t* ctrl = P.ctrl;
+    if (threadIdx.x == 0) {
+        if (P.d_sched) {
+            const uint32_t w = P.d_sched[1];
+            s_sched[0] = w == 8 ? 3u : w == 16 ? 4u : 5u;
+            s_sched[1] = P.d_sched[2];
+            s_sched[2] = P.d_sched[3];
+        } else {
+            s_sched[0] = P.cw_shift;
+            s_sched[1] = P.compact_num;
+            s_sched[2] = P.recount_num;
+        }
+    }
+    __syncthreads();
     unsigned long long* chunk_ctr = reinterpret_cast<unsigned long long*>(ctrl + kPChunks);
     const uint32_t nblocks = gridDim.x;
     const uint32_t lane = lane_id();
@@ -464,7 +486,7 @@ __global__ void __launch_bounds__(kPeelThreads, kBlocksPerSm) k_peel(PeelParams 
             ctrl[kPBigCount + ((rr + 1) & 3)] = ctrl[kPEdges + ((rr + 1) & 3)] = 0;
         }
         // compact the rows once the alive edges have dropped enough since the last compaction
-        if ((uint64_t)live * 100 < (uint64_t)live_at_compaction * P.compact_num) {
+        if ((uint64_t)live * 100 < (uint64_t)live_at_compaction * compact_num()) {
             compact_rows(P, r, warp_cnt);
             if (!grid_barrier(ctrl, nblocks, phase_wait)) return;
             KT_PHASE(3)
@@ -565,7 +587,7 @@ __global__ void __launch_bounds__(kPeelThreads, kBlocksPerSm) k_peel(PeelParams 
                     P.round_level[rounds] = k;
                 }
             }
-            const bool recount = P.recount_num != 0 && (uint64_t)E * 100 >= (uint64_t)P.recount_num * live;
+            const bool recount = recount_num() != 0 && (uint64_t)E * 100 >= (uint64_t)recount_num() * live;
             if (leader) phase_ns[8] = phase_ns[6];
             // limit of the barrier that closes the round: base + the round's queued row entries
             const uint64_t round_wait =
@@ -595,8 +617,8 @@ __global__ void __launch_bounds__(kPeelThreads, kBlocksPerSm) k_peel(PeelParams 
             // entries
             {
                 const uint4* ch = P.ch[r & 1];
-                const uint32_t per_warp = 32u >> P.cw_shift, pos = lane & ((1u << P.cw_shift) - 1);
-                const uint32_t mine = lane >> P.cw_shift;
+                const uint32_t per_warp = 32u >> cw_shift(), pos = lane & ((1u << cw_shift()) - 1);
+                const uint32_t mine = lane >> cw_shift();
                 for (uint32_t c0 = gwarp * per_warp; c0 < C; c0 += nwarps * per_warp) {
                     const uint32_t c = c0 + mine;
                     const uint4 d = c < C ? ch[c] : make_uint4(kNullChunk, 0, 0, 0);
@@ -675,7 +697,7 @@ __global__ void k_barrier_probe(uint32_t* ctrl, uint64_t timeout_ns) {
 
 __global__ void k_init_peel_ctrl(uint32_t* ctrl) {
     const uint32_t i = threadIdx.x;
-    if ((i >= kPBarCount && i < kCtrlWords) || (i >= kPRoundWalk && i < kPRoundWalk + 8))
+    if ((i >= kPBarCount && i < kPSched) || (i >= kPRoundWalk && i < kPRoundWalk + 8))
         ctrl[i] = (i >= kPLMin && i < kPLMin + 4) || (i >= kPLMinId && i < kPLMinId + 4) ? 0xffffffffu : 0u;
 }
 
@@ -795,6 +817,7 @@ int launch_peel(kt_engine* e, uint32_t single_k) {
     P.compact_num = e->sched.compact_percent;
     P.recount_num = e->sched.recount_percent;
     P.single_k = single_k;
+    P.d_sched = e->sched_on_device ? e->ctrl + kPSched : nullptr;
     P.wait_base_ns = e->wait_base_ns;
     P.wait_ns_per_unit = e->wait_ns_per_unit;
     void* args[] = {&P};
@@ -928,6 +951,12 @@ int finish_stats(kt_engine* e) {
     e->stats.num_levels = m ? e->h_ctrl[kPLevels] : 0;
     e->stats.compactions = e->h_ctrl[kPCompactions];
     e->stats.walk_entries = (uint64_t)e->h_ctrl[kPWalk + 1] << 32 | e->h_ctrl[kPWalk];
+    if (e->sched_on_device) {  // the schedule the selector chose on the device for this call
+        e->sched.support_group = e->h_ctrl[kPSched];
+        e->sched.chunk_width = e->h_ctrl[kPSched + 1];
+        e->sched.compact_percent = e->h_ctrl[kPSched + 2];
+        e->sched.recount_percent = e->h_ctrl[kPSched + 3];
+    }
     e->stats.peel_kernel_ms = 0;
     if (e->peel_timed &&
         (rc = check_cuda(cudaEventElapsedTime(&e->stats.peel_kernel_ms, e->ev_peel0, e->ev_peel1), "elapsed time")))

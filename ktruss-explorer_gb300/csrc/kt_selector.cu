@@ -237,7 +237,7 @@ __global__ void k_edge_stats(const uint32_t* __restrict__ s_ptr, const uint32_t*
 // The 16 features from the statistics; with P, also the selector's choice for them.
 __global__ void __launch_bounds__(H) k_features(const unsigned long long* __restrict__ st, uint32_t n, uint32_t m,
                                                 const float* __restrict__ P, float* __restrict__ feat,
-                                                uint32_t* __restrict__ choice) {
+                                                uint32_t* __restrict__ choice, uint32_t* __restrict__ sched) {
     __shared__ float fs[F], xs[F], h1s[H], h2s[H], os[O];
     const int j = threadIdx.x;
     if (j == 0) {
@@ -270,7 +270,12 @@ __global__ void __launch_bounds__(H) k_features(const unsigned long long* __rest
     __syncthreads();
     if (!P) return;
     forward(P, xs, h1s, h2s, os);
-    if (j == 0) *choice = choose(os);
+    if (j == 0) {
+        const uint32_t c = choose(os);
+        *choice = c;
+        // the chosen schedule for the support and peel kernels of this call (ctrl[kPSched..+3])
+        grid_schedule(c, sched, sched + 1, sched + 2, sched + 3);
+    }
 }
 
 // Labels from one graph's timings (kt_schedule_grid order, index = variant * 2 + recount).
@@ -369,21 +374,18 @@ int batch_gradient(kt_selector* s, TrainBuffers& tb, const uint32_t* order, uint
 
 }  // namespace sel
 
+// With a selector attached: the features and the network's choice are computed on the device, and
+// the choice is written to the control block, where the support count and the peel read it - the
+// call enqueues its whole pipeline without waiting for the choice (no host read).  The host learns
+// the chosen schedule when the statistics are read (finish_stats).
 int select_schedule(kt_engine* e) {
+    e->sched_on_device = false;
     kt_selector* s = e->selector;
-    if (!s || e->m == 0 || e->trusted) return KT_OK;  // a trusted run keeps the schedule chosen before
+    if (!s || e->m == 0) return KT_OK;
     if (s->device != e->device) return fail(KT_ERR_INVALID_ARG, "the selector lives on another device");
     int rc;
     if ((rc = graph_features(e, s->d_params))) return rc;
-    uint32_t choice = 0;
-    if ((rc = check_cuda(cudaMemcpyAsync(&choice, e->sel_choice, sizeof(uint32_t), cudaMemcpyDeviceToHost, e->stream),
-                         "read the selector's choice")) ||
-        (rc = check_cuda(cudaStreamSynchronize(e->stream), "synchronize")))
-        return rc;
-    kt_schedule grid[KT_SELECTOR_SCHEDULES];
-    kt_schedule_grid(grid, KT_SELECTOR_SCHEDULES);
-    if (choice >= KT_SELECTOR_SCHEDULES) return fail(KT_ERR_INTERNAL, "selector choice %u out of range", choice);
-    e->sched = grid[choice];
+    e->sched_on_device = true;
     return KT_OK;
 }
 
@@ -402,7 +404,8 @@ int graph_features(kt_engine* e, const float* d_params) {
         count_launch(e);
         if ((rc = check_launch(e, "k_edge_stats"))) return rc;
     }
-    sel::k_features<<<1, sel::H, 0, e->stream>>>(st, e->n, e->m, d_params, e->sel_feat, e->sel_choice);
+    sel::k_features<<<1, sel::H, 0, e->stream>>>(st, e->n, e->m, d_params, e->sel_feat, e->sel_choice,
+                                                 e->ctrl + kPSched);
     count_launch(e);
     return check_launch(e, "k_features");
 }

@@ -25,6 +25,8 @@
 // warps (a warp-private table), all others as ranges of at most kHeavyIn in-edges to whole blocks
 // (a block table); rows longer than the block table are searched in HBM instead of hashed.
 
+#include <algorithm>
+
 #include "kt_device.cuh"
 #include "kt_engine.h"
 
@@ -35,10 +37,9 @@ namespace {
 constexpr int kThreads = 256;
 
 template <int G>
-__global__ void __launch_bounds__(kThreads) k_support(const uint32_t* __restrict__ o_ptr,
-                                                      const uint32_t* __restrict__ o_col,
-                                                      const uint32_t* __restrict__ e_src, uint32_t m,
-                                                      uint32_t* __restrict__ sup) {
+__device__ __forceinline__ void support_body(const uint32_t* __restrict__ o_ptr, const uint32_t* __restrict__ o_col,
+                                             const uint32_t* __restrict__ e_src, uint32_t m,
+                                             uint32_t* __restrict__ sup) {
     const uint32_t lane = lane_id();
     const uint32_t glane = lane & (G - 1);
     const uint32_t gmask = (G == 32) ? kFullMask : (((1u << G) - 1) << (lane & ~(uint32_t)(G - 1)));
@@ -71,6 +72,29 @@ __global__ void __launch_bounds__(kThreads) k_support(const uint32_t* __restrict
 #pragma unroll
         for (int o = G / 2; o > 0; o >>= 1) cnt += __shfl_xor_sync(gmask, cnt, o);
         if (glane == 0 && cnt) atomicAdd(&sup[j], cnt);
+    }
+}
+
+template <int G>
+__global__ void __launch_bounds__(kThreads) k_support(const uint32_t* __restrict__ o_ptr,
+                                                      const uint32_t* __restrict__ o_col,
+                                                      const uint32_t* __restrict__ e_src, uint32_t m,
+                                                      uint32_t* __restrict__ sup) {
+    support_body<G>(o_ptr, o_col, e_src, m, sup);
+}
+
+// The same count with the lane group read from the control block, where the learned selector's
+// inference kernel wrote its choice: the schedule is chosen on the device, with no host read.
+__global__ void __launch_bounds__(kThreads) k_support_chosen(const uint32_t* __restrict__ o_ptr,
+                                                             const uint32_t* __restrict__ o_col,
+                                                             const uint32_t* __restrict__ e_src, uint32_t m,
+                                                             const uint32_t* __restrict__ sched,
+                                                             uint32_t* __restrict__ sup) {
+    switch (sched[0]) {
+        case 4: support_body<4>(o_ptr, o_col, e_src, m, sup); break;
+        case 16: support_body<16>(o_ptr, o_col, e_src, m, sup); break;
+        case 32: support_body<32>(o_ptr, o_col, e_src, m, sup); break;
+        default: support_body<8>(o_ptr, o_col, e_src, m, sup); break;
     }
 }
 
@@ -324,6 +348,15 @@ int count_support(kt_engine* e) {
     if (e->m == 0) return KT_OK;
     int rc = check_cuda(cudaMemsetAsync(e->sup, 0, sizeof(uint32_t) * e->m, e->stream), "clear support");
     if (rc) return rc;
+    if (e->sched_on_device) {
+        // any group the selector may choose (4, 8 or 16 lanes per edge) fits this grid
+        const uint64_t blocks = std::min<uint64_t>(((uint64_t)e->m * 16 + kThreads - 1) / kThreads,
+                                                   (uint64_t)e->num_sms * 16);
+        k_support_chosen<<<(uint32_t)blocks, kThreads, 0, e->stream>>>(e->o_ptr, e->o_col, e->e_src, e->m,
+                                                                       e->ctrl + kPSched, e->sup);
+        count_launch(e);
+        return check_launch(e, "k_support_chosen");
+    }
     const uint32_t G = e->sched.support_group;
     if (G == 0) return count_support_hash(e);
     uint64_t blocks = ((uint64_t)e->m * G + kThreads - 1) / kThreads;

@@ -129,6 +129,41 @@ def test_decompositions_with_selector_are_exact():
     eng.set_selector(None)
 
 
+def test_selector_choice_stays_on_the_device_and_replays_as_a_graph():
+    """With a selector attached the schedule is chosen on the device: a decomposition enqueued
+    without synchronizing gives the oracle's result, the engine reports the choice once the call has
+    finished, and repeat runs capture the whole pipeline - features, inference, support count and
+    peel - as one CUDA graph."""
+    torch = pytest.importorskip("torch")
+    s = kt.Selector(0, seed=12)
+    rng = np.random.default_rng(8)
+    s.set_params(params=rng.normal(0, 0.5, so.NPARAMS))
+    eng = kt.Engine(0)
+    eng.set_selector(s)
+    n, u, v = kt.plant_cliques(*kt.gen_ba(8000, 6, 13), 2, 30, 50, 14)
+    src, dst = both_directions(u, v)
+    d_src = torch.from_numpy(src.view(np.int32)).cuda()
+    d_dst = torch.from_numpy(dst.view(np.int32)).cuda()
+    d_out = torch.empty(len(src), dtype=torch.int32, device="cuda")
+    d_k = torch.zeros(1, dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    eng.decompose(d_src.data_ptr(), d_dst.data_ptr(), len(src), n, d_out.data_ptr(), d_k.data_ptr(), sync=False)
+    st = eng.stats()  # waits for the call; the schedule it ran with is the device's choice
+    ref = oracle.decompose(n, src, dst, method="peel")
+    assert int(d_k.item()) == ref["k_max"] and np.array_equal(d_out.cpu().numpy().view(np.uint32), ref["truss"])
+    feats = eng.features(d_src.data_ptr(), d_dst.data_ptr(), len(src), n)
+    assert eng.schedule().as_tuple() == s.predict(feats)[0].as_tuple()
+    assert st.k_max == ref["k_max"]
+    first = d_out.clone()
+    eng.decompose(d_src.data_ptr(), d_dst.data_ptr(), len(src), n, d_out.data_ptr(), d_k.data_ptr())
+    eng.replay()
+    eng.replay()
+    assert eng.replay_mode() == "cuda graph"
+    assert torch.equal(d_out, first)
+    eng.set_selector(None)
+    eng.close()
+
+
 DATA = sel_mod.DATA
 HAVE_DATA = all(os.path.exists(os.path.join(DATA, f)) for f in ("selector_train.npz", "selector_heldout.npz"))
 
