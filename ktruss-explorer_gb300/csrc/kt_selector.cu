@@ -16,6 +16,7 @@
 // fastest recount-on schedule beats the fastest recount-off one.  Every schedule computes the
 // same truss numbers, so a wrong prediction costs time, never correctness.
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <numeric>
@@ -174,11 +175,12 @@ __global__ void __launch_bounds__(H) k_predict(const float* __restrict__ P, cons
 // Graph statistics (integers, exact): per vertex (rank space) degree d and oriented out-degree
 // od; per edge the walk length min(d_u, d_v).
 enum : int {
-    kSumD2 = 0, kMaxD, kLowD, kHighD, kMaxOd, kSumOd2, kSumMin, kSumMin2, kShortMin, kLongMin, kStats = 16
+    kSumD2 = 0, kMaxD, kLowD, kHighD, kMaxOd, kSumOd2, kSumMin, kSumMin2, kShortMin, kLongMin, kTicket = 15,
+    kStats = 16
 };
 
-__global__ void k_vertex_stats(const uint32_t* __restrict__ s_ptr, const uint32_t* __restrict__ o_ptr, uint32_t n,
-                               unsigned long long* __restrict__ st) {
+__device__ __forceinline__ void vertex_stats(const uint32_t* __restrict__ s_ptr, const uint32_t* __restrict__ o_ptr,
+                                             uint32_t n, unsigned long long* __restrict__ st) {
     unsigned long long d2 = 0, od2 = 0, low = 0, high = 0;
     uint32_t maxd = 0, maxod = 0;
     for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
@@ -208,8 +210,9 @@ __global__ void k_vertex_stats(const uint32_t* __restrict__ s_ptr, const uint32_
     }
 }
 
-__global__ void k_edge_stats(const uint32_t* __restrict__ s_ptr, const uint32_t* __restrict__ e_src,
-                             const uint32_t* __restrict__ o_col, uint32_t m, unsigned long long* __restrict__ st) {
+__device__ __forceinline__ void edge_stats(const uint32_t* __restrict__ s_ptr, const uint32_t* __restrict__ e_src,
+                                           const uint32_t* __restrict__ o_col, uint32_t m,
+                                           unsigned long long* __restrict__ st) {
     unsigned long long s1 = 0, s2 = 0, shrt = 0, lng = 0;
     for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < m; j += gridDim.x * blockDim.x) {
         const uint32_t u = e_src[j], v = o_col[j];
@@ -234,11 +237,25 @@ __global__ void k_edge_stats(const uint32_t* __restrict__ s_ptr, const uint32_t*
     }
 }
 
-// The 16 features from the statistics; with P, also the selector's choice for them.
-__global__ void __launch_bounds__(H) k_features(const unsigned long long* __restrict__ st, uint32_t n, uint32_t m,
-                                                const float* __restrict__ P, float* __restrict__ feat,
-                                                uint32_t* __restrict__ choice, uint32_t* __restrict__ sched) {
+// Statistics, features and choice in one launch of H-thread blocks: every block adds its share of
+// the vertex and edge statistics; the last block to finish (an atomic ticket in st[kTicket], after a
+// fence) turns them into the 16 features and, with P, runs the network and writes the choice and
+// its schedule.  st must be zero on entry.
+__global__ void __launch_bounds__(H) k_select(const uint32_t* __restrict__ s_ptr, const uint32_t* __restrict__ o_ptr,
+                                              const uint32_t* __restrict__ e_src, const uint32_t* __restrict__ o_col,
+                                              uint32_t n, uint32_t m, unsigned long long* __restrict__ st,
+                                              const float* __restrict__ P, float* __restrict__ feat,
+                                              uint32_t* __restrict__ choice, uint32_t* __restrict__ sched) {
     __shared__ float fs[F], xs[F], h1s[H], h2s[H], os[O];
+    __shared__ uint32_t last;
+    vertex_stats(s_ptr, o_ptr, n, st);
+    edge_stats(s_ptr, e_src, o_col, m, st);
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(st + kTicket, 1ull) == gridDim.x - 1;
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
     const int j = threadIdx.x;
     if (j == 0) {
         const double dn = n > 0 ? (double)n : 1.0, dm = m > 0 ? (double)m : 1.0;
@@ -393,21 +410,15 @@ int graph_features(kt_engine* e, const float* d_params) {
     unsigned long long* st = reinterpret_cast<unsigned long long*>(e->sel_stats);
     int rc = check_cuda(cudaMemsetAsync(st, 0, sizeof(unsigned long long) * sel::kStats, e->stream), "clear statistics");
     if (rc) return rc;
-    const uint32_t blocks = (uint32_t)e->num_sms * 4;
-    if (e->n) {
-        sel::k_vertex_stats<<<blocks, 256, 0, e->stream>>>(e->s_ptr, e->o_ptr, e->n, st);
-        count_launch(e);
-        if ((rc = check_launch(e, "k_vertex_stats"))) return rc;
-    }
-    if (e->m) {
-        sel::k_edge_stats<<<blocks, 256, 0, e->stream>>>(e->s_ptr, e->e_src, e->o_col, e->m, st);
-        count_launch(e);
-        if ((rc = check_launch(e, "k_edge_stats"))) return rc;
-    }
-    sel::k_features<<<1, sel::H, 0, e->stream>>>(st, e->n, e->m, d_params, e->sel_feat, e->sel_choice,
-                                                 e->ctrl + kPSched);
+    // one launch: enough 64-thread blocks to cover the larger of n and m once per thread, at most
+    // 16 per SM
+    const uint64_t work = std::max<uint64_t>(e->n, e->m);
+    const uint32_t blocks =
+        (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((work + sel::H - 1) / sel::H, (uint64_t)e->num_sms * 16));
+    sel::k_select<<<blocks, sel::H, 0, e->stream>>>(e->s_ptr, e->o_ptr, e->e_src, e->o_col, e->n, e->m, st, d_params,
+                                                    e->sel_feat, e->sel_choice, e->ctrl + kPSched);
     count_launch(e);
-    return check_launch(e, "k_features");
+    return check_launch(e, "k_select");
 }
 
 }  // namespace kt

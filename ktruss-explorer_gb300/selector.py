@@ -3,6 +3,7 @@
     python ktruss-explorer_gb300/selector.py collect --count 2000 --seed 1 --out data/selector_train.npz
     python ktruss-explorer_gb300/selector.py collect --count 200 --seed 2 --out data/selector_heldout.npz
     python ktruss-explorer_gb300/selector.py collect --families batch --count 300 --seed 3 --out data/selector_batch.npz
+    python ktruss-explorer_gb300/selector.py collect --families large --count 24 --seed 4 --out data/selector_large.npz
     python ktruss-explorer_gb300/selector.py evaluate
 
 `collect` generates seeded graphs - Erdos-Renyi, R-MAT scale 12-18, Barabasi-Albert, random
@@ -32,6 +33,9 @@ FAMILIES = ("er", "rmat", "ba", "rgg", "cliques")
 # Unions of 16-128 graphs of the batch distribution (kt_gen_batch), as kt_engine_decompose_batch
 # sees them: a separate training set, so that the network also knows batches.
 BATCH_FAMILIES = ("batch",)
+# Large R-MAT graphs (scale 19-23, edge factor 16 or 32, half of them with planted cliques): a
+# separate training set where the oriented rows meet hubs of hundreds of thousands of neighbours.
+LARGE_FAMILIES = ("rmat_large",)
 
 
 def graph_spec(index: int, seed: int, families=FAMILIES) -> dict:
@@ -43,6 +47,9 @@ def graph_spec(index: int, seed: int, families=FAMILIES) -> dict:
                     seed=int(rng.integers(1, 2**31)))
     gseed = int(rng.integers(1, 2**31))
     logn = lambda lo, hi: int(round(2 ** rng.uniform(lo, hi)))
+    if fam == "rmat_large":
+        return dict(family=fam, scale=int(rng.integers(19, 24)), ef=int(rng.choice([16, 32])),
+                    cliques=int(rng.choice([0, 8])), seed=gseed)
     if fam == "er":
         return dict(family=fam, n=logn(11, 17), degree=float(rng.uniform(4, 32)), seed=gseed)
     if fam == "rmat":
@@ -67,6 +74,9 @@ def make_graph(spec: dict):
         return kt.gen_er(n, spec["degree"] / (n - 1), spec["seed"])
     if f == "rmat":
         return kt.gen_rmat(spec["scale"], spec["ef"], 0.57, 0.19, 0.19, spec["seed"])
+    if f == "rmat_large":
+        g = kt.gen_rmat(spec["scale"], spec["ef"], 0.57, 0.19, 0.19, spec["seed"])
+        return kt.plant_cliques(*g, spec["cliques"], 64, 256, spec["seed"] + 1) if spec["cliques"] else g
     if f == "ba":
         return kt.gen_ba(spec["n"], spec["m"], spec["seed"])
     if f == "rgg":
@@ -119,12 +129,14 @@ def load(path: str) -> dict:
 
 
 def load_training() -> dict:
-    """The training data in data/: the 2000 single graphs, plus the batch unions when present."""
+    """The training data in data/: the 2000 single graphs, plus the batch unions and the large
+    R-MAT graphs when present."""
     d = load(os.path.join(DATA, "selector_train.npz"))
-    extra = os.path.join(DATA, "selector_batch.npz")
-    if os.path.exists(extra):
-        b = load(extra)
-        d = {k: np.concatenate([d[k], b[k]]) for k in ("features", "times", "specs", "edges")}
+    for name in ("selector_batch.npz", "selector_large.npz"):
+        extra = os.path.join(DATA, name)
+        if os.path.exists(extra):
+            b = load(extra)
+            d = {k: np.concatenate([d[k], b[k]]) for k in ("features", "times", "specs", "edges")}
     return d
 
 
@@ -159,15 +171,16 @@ def main():
     c.add_argument("--seed", type=int, default=1)
     c.add_argument("--repeats", type=int, default=1)
     c.add_argument("--out", required=True)
-    c.add_argument("--families", default="graphs", choices=["graphs", "batch"],
-                   help="graphs: ER, R-MAT, BA, RGG, planted cliques; batch: unions of batch graphs")
+    c.add_argument("--families", default="graphs", choices=["graphs", "batch", "large"],
+                   help="graphs: ER, R-MAT, BA, RGG, planted cliques; batch: unions of batch graphs; "
+                        "large: R-MAT scale 19-23")
     e = sub.add_parser("evaluate")
     e.add_argument("--train", default=None, help="training set (default: data/, with the batch unions)")
     e.add_argument("--heldout", default=os.path.join(DATA, "selector_heldout.npz"))
     e.add_argument("--epochs", type=int, default=300)
     args = ap.parse_args()
     if args.cmd == "collect":
-        fams = BATCH_FAMILIES if args.families == "batch" else FAMILIES
+        fams = {"batch": BATCH_FAMILIES, "large": LARGE_FAMILIES}.get(args.families, FAMILIES)
         d = collect(args.count, args.seed, repeats=args.repeats, log=lambda s: print(s, flush=True), families=fams)
         save(args.out, d)
         print(f"wrote {args.out}: {args.count} graphs", flush=True)
