@@ -539,6 +539,7 @@ def run_batch(args, world, rank, local):
                                    "one call", "n": n, "m": m, "edges_per_s": m * world / (ms * 1e-3),
                        "k_max_max": int(kmax.max()), "peel_rounds": st.num_rounds, "peel_levels": st.num_levels,
                        "phase_ms": {"build": st.build_ms, "support": st.support_ms, "peel": st.peel_ms},
+                       "peel_phase_ms": st.as_dict()["peel_phase_ms"], "walk_entries": st.walk_entries,
                        "generation_s": gen_s,
                        "parallelism": f"graph shards x{world}" if world > 1 else "one GPU", "schedule": sched,
                        "single_graph_path": single,
