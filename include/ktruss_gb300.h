@@ -174,8 +174,8 @@ typedef struct kt_stats {
                                     collection, row compaction, mark, process), barrier to
                                     barrier, as seen by its first block                        */
     float peel_kernel_ms;        /* CUDA-event time of the peel kernel launch alone            */
-    float select_ms;             /* learned selector: features, inference and the read-back of
-                                    its choice (0 without a selector); part of last_ms         */
+    float select_ms;             /* learned selector: statistics, features and inference, one
+                                    launch (0 without a selector); part of last_ms             */
     uint64_t walk_entries;       /* adjacency entries in the rows of all queued edges: the
                                     decrement work (a round that recounts instead does not walk
                                     its queued rows)                                          */
@@ -183,6 +183,8 @@ typedef struct kt_stats {
                                     time of the input copies host -> device                   */
     float copy_out_ms;           /*   and of the output copies device -> host (plus the emit
                                     of per-graph k_max in a batch)                            */
+    float emit_ms;               /* decompositions: of peel_ms, the per-entry output (truss
+                                    numbers and k_max) after the peel; 0 for other calls       */
 } kt_stats;
 
 /* Schedule of the engine's kernels (no counterpart in the reference, whose tuning knobs are the
@@ -295,7 +297,8 @@ int kt_engine_get_schedule(kt_engine* engine, kt_schedule* schedule);
 
 /* Wait limit of the peel kernel's grid barriers (no counterpart in the reference, whose loop is
  * driven from the host): every wait is bounded by base_ns plus ns_per_unit for each unit of work
- * the wait can legitimately cover - each row entry queued for the round that the barrier closes,
+ * the wait can legitimately cover - each row entry slot of the work chunks queued for the round
+ * that the barrier closes (row entries rounded up to whole chunks),
  * each edge (twice) for a level phase - after which the kernel returns KT_ERR_TIMEOUT instead of
  * waiting forever.  Defaults: 10 s and 8 ns.  base_ns must be at least 1 microsecond. */
 int kt_engine_set_wait_limit(kt_engine* engine, uint64_t base_ns, uint32_t ns_per_unit);
@@ -311,8 +314,8 @@ int kt_get_schedule(kt_schedule* schedule);
  * {8, 16, 32} x compact_percent {0, 85} x recount_percent {0, 50}, peel_blocks 0 (36).  Writes
  * min(36, cap) schedules to `out` (may be NULL) and returns 36. */
 uint32_t kt_schedule_grid(kt_schedule* out, uint32_t cap);
-/* Autotuner (no counterpart in the reference).  Decomposes the given device graph — or a batch
- * given as the union of its graphs — once per candidate schedule and `repeats` times each
+/* Autotuner (no counterpart in the reference).  Decomposes the given device graph once per
+ * candidate schedule and `repeats` times each
  * (>= 1), and keeps the candidate with the least device time of support count plus peel (CUDA
  * events; the CSR build does not depend on the schedule).  candidates: num_candidates schedules,
  * or NULL for the built-in grid.  ms (optional): the least time of each candidate.  On return the
@@ -321,6 +324,13 @@ uint32_t kt_schedule_grid(kt_schedule* out, uint32_t cap);
 int kt_engine_autotune(kt_engine* engine, const uint32_t* d_src, const uint32_t* d_dst, uint64_t num_entries,
                        uint32_t num_nodes, const kt_schedule* candidates, uint32_t num_candidates,
                        uint32_t repeats, float* ms, kt_schedule* best);
+/* The same for batches: times each candidate the way kt_engine_decompose_batch runs it, on the
+ * union of a sample batch's graphs (d_src/d_dst/num_nodes as for that call).  A batch's peel
+ * always runs one block per SM, while a single graph of the same size whose oriented CSR outgrows
+ * L2 runs two (peel_blocks 0), so tuning a large union as one graph measures another kernel. */
+int kt_engine_autotune_batch(kt_engine* engine, const uint32_t* d_src, const uint32_t* d_dst,
+                             uint64_t num_entries, uint32_t num_nodes, const kt_schedule* candidates,
+                             uint32_t num_candidates, uint32_t repeats, float* ms, kt_schedule* best);
 /* ---- symmetrize and deduplicate ----------------------------------------------------------
  * Turns an arbitrary entry list on the device (one or both directions, duplicates, self loops)
  * into the symmetric simple graph the k-truss calls take: each undirected edge {u, v}, u != v,

@@ -25,9 +25,8 @@ enum : uint32_t {
 // Layout of the device control block (uint32 words unless noted).
 enum : uint32_t {
     kCtrlError = 0,
-    // words 1, 12, 13 and 26-27 are unused; 21-24 hold the support plan during the count
+    // words 1-9, 12, 13 and 26-27 are unused; 21-24 hold the support plan during the count
     kCtrlVariantChanged = 25,  // a variant pass deleted an edge
-    kPRoundWalk = 2,      // [4] u64 (words 2..9): row entries queued for the round (wait limits)
     kCtrlTriLo = 10,      // 64-bit triangle counter (lo, hi)
     kCtrlTriHi = 11,
     kCtrlBigRow = 14,     // first rank whose symmetric row is long (block-wide compaction)

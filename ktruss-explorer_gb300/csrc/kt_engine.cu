@@ -85,6 +85,7 @@ size_t carve(kt_engine* e, char* base, uint32_t n, uint64_t N, bool staging) {
     e->level_ns = c.take<uint32_t>(e->cap_levels);
     e->level_front = c.take<uint32_t>(e->cap_levels);
     e->sel_stats = c.take<uint32_t>(32);
+    e->sel_part = c.take<uint64_t>((size_t)kSelMaxBlocks * 10);
     e->sel_feat = c.take<float>(KT_SELECTOR_FEATURES);
     e->sel_choice = c.take<uint32_t>(1);
     e->hist = c.take<uint32_t>(hist_words);
@@ -146,6 +147,9 @@ int reserve(kt_engine* e, uint32_t max_nodes, uint64_t max_entries) {
     e->arena = p;
     e->arena_bytes = bytes;
     carve(e, static_cast<char*>(p), max_nodes, max_entries, true);
+    // the selector's block ticket starts at zero; its last block clears it again on every call
+    if ((rc = check_cuda(cudaMemsetAsync(e->sel_stats, 0, sizeof(uint32_t) * 32, e->stream), "clear ticket")))
+        return rc;
     e->cap_nodes = max_nodes;
     e->cap_entries = max_entries;
     return KT_OK;
@@ -176,7 +180,10 @@ double now_ms() {
     return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
 
-int record_start(kt_engine* e) { return check_cuda(cudaEventRecord(e->ev_start, e->stream), "record start"); }
+int record_start(kt_engine* e) {
+    e->emit_timed = false;
+    return check_cuda(cudaEventRecord(e->ev_start, e->stream), "record start");
+}
 
 int record(kt_engine* e, cudaEvent_t ev) { return check_cuda(cudaEventRecord(ev, e->stream), "record event"); }
 
@@ -195,6 +202,11 @@ int record_stop(kt_engine* e) {
     e->stats.support_ms = b;
     e->stats.peel_ms = c;
     e->stats.last_ms = a + b + c + d;
+    e->stats.emit_ms = 0;
+    if (e->emit_timed &&
+        (rc = check_cuda(cudaEventElapsedTime(&e->stats.emit_ms, e->ev_peeled, e->ev_stop), "elapsed time")))
+        return rc;
+    e->emit_timed = false;
     return KT_OK;
 }
 
@@ -225,6 +237,8 @@ int run_decompose(kt_engine* e, const uint32_t* d_src, const uint32_t* d_dst, ui
     if ((rc = kt::count_support(e))) return rc;
     if ((rc = record(e, e->ev_counted))) return rc;
     if ((rc = kt::peel_decompose(e))) return rc;
+    if ((rc = record(e, e->ev_peeled))) return rc;
+    e->emit_timed = true;
     if ((rc = kt::emit_truss_per_entry(e, d_truss, d_k_max))) return rc;
     if ((rc = record_stop(e))) return rc;
     return fill_graph_stats(e);
@@ -371,6 +385,7 @@ int kt_engine_create(int device, kt_engine** out) {
         (rc = check_cuda(cudaEventCreate(&e->ev_built), "create event")) ||
         (rc = check_cuda(cudaEventCreate(&e->ev_counted), "create event")) ||
         (rc = check_cuda(cudaEventCreate(&e->ev_select), "create event")) ||
+        (rc = check_cuda(cudaEventCreate(&e->ev_peeled), "create event")) ||
         (rc = check_cuda(cudaEventCreate(&e->ev_copy[0]), "create event")) ||
         (rc = check_cuda(cudaEventCreate(&e->ev_copy[1]), "create event")) ||
         (rc = check_cuda(cudaEventCreate(&e->ev_copy[2]), "create event")) ||
@@ -401,6 +416,7 @@ int kt_engine_destroy(kt_engine* e) {
     if (e->ev_built) cudaEventDestroy(e->ev_built);
     if (e->ev_counted) cudaEventDestroy(e->ev_counted);
     if (e->ev_select) cudaEventDestroy(e->ev_select);
+    if (e->ev_peeled) cudaEventDestroy(e->ev_peeled);
     for (cudaEvent_t ev : e->ev_copy)
         if (ev) cudaEventDestroy(ev);
     if (e->ev_peel0) cudaEventDestroy(e->ev_peel0);
@@ -577,9 +593,11 @@ uint32_t kt_schedule_grid(kt_schedule* out, uint32_t cap) {
     return count;
 }
 
-int kt_engine_autotune(kt_engine* e, const uint32_t* d_src, const uint32_t* d_dst, uint64_t num_entries,
-                       uint32_t num_nodes, const kt_schedule* candidates, uint32_t num_candidates, uint32_t repeats,
-                       float* ms, kt_schedule* best) {
+namespace {
+
+int autotune(kt_engine* e, const uint32_t* d_src, const uint32_t* d_dst, uint64_t num_entries, uint32_t num_nodes,
+             const kt_schedule* candidates, uint32_t num_candidates, uint32_t repeats, float* ms, kt_schedule* best,
+             bool batch) {
     kt::clear_error();
     if (!e) return fail(KT_ERR_INVALID_ARG, "kt_engine_autotune: null engine");
     if (num_entries && (!d_src || !d_dst)) return fail(KT_ERR_INVALID_ARG, "kt_engine_autotune: null buffer");
@@ -596,6 +614,7 @@ int kt_engine_autotune(kt_engine* e, const uint32_t* d_src, const uint32_t* d_ds
     if (rc) return rc;
     uint32_t best_i = 0;
     float best_ms = 0;
+    e->batch_call = batch;  // the peel's launch shape follows the call being tuned
     for (uint32_t i = 0; i < num_candidates; ++i) {
         if ((rc = kt_engine_set_schedule(e, &candidates[i]))) break;
         float t_min = 0;
@@ -618,6 +637,7 @@ int kt_engine_autotune(kt_engine* e, const uint32_t* d_src, const uint32_t* d_ds
             best_i = i;
         }
     }
+    e->batch_call = false;
     if (rc) {
         e->sched = saved;
         return rc;
@@ -625,6 +645,20 @@ int kt_engine_autotune(kt_engine* e, const uint32_t* d_src, const uint32_t* d_ds
     e->sched = candidates[best_i];
     if (best) *best = candidates[best_i];
     return KT_OK;
+}
+
+}  // namespace
+
+int kt_engine_autotune(kt_engine* e, const uint32_t* d_src, const uint32_t* d_dst, uint64_t num_entries,
+                       uint32_t num_nodes, const kt_schedule* candidates, uint32_t num_candidates, uint32_t repeats,
+                       float* ms, kt_schedule* best) {
+    return autotune(e, d_src, d_dst, num_entries, num_nodes, candidates, num_candidates, repeats, ms, best, false);
+}
+
+int kt_engine_autotune_batch(kt_engine* e, const uint32_t* d_src, const uint32_t* d_dst, uint64_t num_entries,
+                             uint32_t num_nodes, const kt_schedule* candidates, uint32_t num_candidates,
+                             uint32_t repeats, float* ms, kt_schedule* best) {
+    return autotune(e, d_src, d_dst, num_entries, num_nodes, candidates, num_candidates, repeats, ms, best, true);
 }
 
 int kt_engine_tiled_coocsr(kt_engine* e, const uint32_t* d_src, const uint32_t* d_dst, uint64_t num_entries,

@@ -8,6 +8,9 @@
 
 #include "kt_internal.h"
 
+// Most blocks of the selector's statistics launch (its per-block partials buffer).
+constexpr uint32_t kSelMaxBlocks = 1024;
+
 struct kt_engine {
     int device = 0;
     int num_sms = 0;
@@ -16,6 +19,8 @@ struct kt_engine {
     cudaEvent_t ev_select = nullptr;  // after the build, before the selector's choice
     cudaEvent_t ev_copy[4] = {};      // host-buffer calls: around the input and output copies
     cudaEvent_t ev_peel0 = nullptr, ev_peel1 = nullptr;  // around the peel kernel launch
+    cudaEvent_t ev_peeled = nullptr;  // decompositions: after the peel, before the per-entry output
+    bool emit_timed = false;          // ev_peeled was recorded in this call
     bool peel_timed = false;
     uint64_t launches = 0;
 
@@ -99,7 +104,8 @@ struct kt_engine {
     bool batch_call = false;           // the current call decomposes a batch of separate graphs
     kt_selector* selector = nullptr;   // learned schedule selector (kt_engine_set_selector)
     bool sched_on_device = false;      // this call's schedule is the selector's choice in ctrl[kPSched]
-    uint32_t* sel_stats = nullptr;     // 16 u64 graph statistics for the selector's features
+    uint32_t* sel_stats = nullptr;     // 16 u64: the selector's block ticket (word kTicket)
+    uint64_t* sel_part = nullptr;      // per-block partial statistics (kSelMaxBlocks x 10 u64)
     float* sel_feat = nullptr;         // the 16 features
     uint32_t* sel_choice = nullptr;    // the selector's schedule index
     kt_stats stats{};

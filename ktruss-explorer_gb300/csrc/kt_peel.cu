@@ -35,10 +35,11 @@
 //
 // Every grid barrier wait is bounded: by the engine's base limit (kt_engine_set_wait_limit, 10 s by
 // default) plus a share proportional to the work the wait can legitimately cover - per row entry
-// queued for the round that the barrier closes, per edge for the level phases (scans, compaction,
+// slot of the chunks queued for the round that the barrier closes, per edge for the level phases (scans, compaction,
 // recount) - so a long legitimate round on a large graph is not cut short.  On expiry the kernel
 // reports KT_ERR_TIMEOUT through the control block and returns.
 
+#include <algorithm>
 #include <cstdlib>
 #include <vector>
 
@@ -53,7 +54,20 @@ constexpr int kThreads = 256;          // helper kernels
 #ifndef KT_PEEL_THREADS
 #define KT_PEEL_THREADS 1024
 #endif
-constexpr int kPeelThreads = KT_PEEL_THREADS;  // persistent kernel: one or two blocks per SM
+constexpr int kPeelThreads = KT_PEEL_THREADS;  // persistent kernel, one block per SM ...
+#ifndef KT_PEEL_WIDE_THREADS
+#define KT_PEEL_WIDE_THREADS 1024
+#endif
+#ifndef KT_PEEL_WIDE_BLOCKS
+#define KT_PEEL_WIDE_BLOCKS 2
+#endif
+constexpr int kWideThreads = KT_PEEL_WIDE_THREADS;  // ... or kWideBlocks blocks of kWideThreads per SM
+constexpr int kWideBlocks = KT_PEEL_WIDE_BLOCKS;
+static_assert(kWideBlocks >= 2, "the wide build has more than one block per SM");
+template <int kBlocksPerSm>
+__host__ __device__ constexpr int peel_threads() {
+    return kBlocksPerSm == 1 ? kPeelThreads : kWideThreads;
+}
 
 inline uint32_t grid_for(uint64_t n, int threads = kThreads) {
     uint64_t b = (n + threads - 1) / threads;
@@ -103,6 +117,14 @@ constexpr uint32_t kDead = 0xffffffffu;  // support of a removed edge
 // The launch's chunk width (log2), compaction and recount percentages, set once per block at the
 // start of k_peel from its parameters or from the device-side schedule choice.
 __shared__ uint32_t s_sched[3];
+// Row entries this block queued for walks over the whole launch (a statistic, added to the control
+// block once when the block finishes, so the pushes pay a shared-memory atomic, not a global one).
+__shared__ unsigned long long s_walk;
+// Edges this block queued since its last barrier and their ring slot (every push between two
+// barriers targets the same round), added to the control block once per block at the barrier.
+__shared__ uint32_t s_edges, s_edge_slot;
+// A level scan's alive count, minimum support and smallest alive edge id over the block's warps.
+__shared__ uint32_t s_lv_alive, s_lv_min, s_lv_min_id;
 __device__ __forceinline__ uint32_t cw_shift() { return s_sched[0]; }
 __device__ __forceinline__ uint32_t compact_num() { return s_sched[1]; }
 __device__ __forceinline__ uint32_t recount_num() { return s_sched[2]; }
@@ -147,9 +169,9 @@ __device__ __forceinline__ void push_edges(const PeelParams& P, uint32_t e, bool
     unsigned long long cb = 0;
     if (lane == 0) {
         cb = atomicAdd(reinterpret_cast<unsigned long long*>(P.ctrl + kPChunks) + slot, (unsigned long long)total);
-        atomicAdd(P.ctrl + kPEdges + slot, __popc(mt));
-        atomicAdd(reinterpret_cast<unsigned long long*>(P.ctrl + kPWalk), (unsigned long long)walked);
-        atomicAdd(reinterpret_cast<unsigned long long*>(P.ctrl + kPRoundWalk) + slot, (unsigned long long)walked);
+        atomicAdd(&s_edges, __popc(mt));
+        s_edge_slot = slot;
+        atomicAdd(&s_walk, (unsigned long long)walked);
     }
     cb = __shfl_sync(kFullMask, cb, 0);
     uint4* ch = P.ch[rr & 1];
@@ -170,6 +192,18 @@ __device__ __forceinline__ void push_edges(const PeelParams& P, uint32_t e, bool
         bb = __shfl_sync(kFullMask, bb, 0);
         if (take) P.big[rr & 1][bb + __popc(mt & lanemask_lt())] = e;
     }
+}
+
+// Grid barrier of the peel: first adds the edges this block queued since its last barrier to
+// their round's count (one atomic per block instead of one per pushing warp).  The arrival's
+// release orders that add before any block reads the count after the barrier.
+__device__ __forceinline__ bool peel_barrier(uint32_t* ctrl, uint32_t nblocks, uint64_t wait_ns) {
+    __syncthreads();
+    if (threadIdx.x == 0 && s_edges) {
+        atomicAdd(ctrl + kPEdges + s_edge_slot, s_edges);
+        s_edges = 0;
+    }
+    return grid_barrier(ctrl, nblocks, wait_ns);
 }
 
 // Entries of a removed edge e's shorter row (vertex x): called by all 32 lanes of a warp
@@ -413,8 +447,8 @@ __device__ __forceinline__ void collect(const PeelParams& P, uint32_t thr, uint3
 // larger graphs, whose walks wait on DRAM.  Measured on GB300: R-MAT 20 (CSR in L2) 89 ms with one
 // block and 99 ms with two; R-MAT 24 (CSR 2 GB) 8.65 s with one and 8.21 s with two.
 template <int kBlocksPerSm>
-__global__ void __launch_bounds__(kPeelThreads, kBlocksPerSm) k_peel(PeelParams P) {
-    __shared__ uint32_t warp_cnt[kPeelThreads / 32];
+__global__ void __launch_bounds__(peel_threads<kBlocksPerSm>(), kBlocksPerSm) k_peel(PeelParams P) {
+    __shared__ uint32_t warp_cnt[peel_threads<kBlocksPerSm>() / 32];
     uint32_t* ctrl = P.ctrl;
     if (threadIdx.x == 0) {
         if (P.d_sched) {
@@ -427,6 +461,10 @@ __global__ void __launch_bounds__(kPeelThreads, kBlocksPerSm) k_peel(PeelParams 
             s_sched[1] = P.compact_num;
             s_sched[2] = P.recount_num;
         }
+        s_walk = 0;
+        s_edges = 0;
+        s_lv_alive = 0;
+        s_lv_min = s_lv_min_id = kDead;
     }
     __syncthreads();
     unsigned long long* chunk_ctr = reinterpret_cast<unsigned long long*>(ctrl + kPChunks);
@@ -455,14 +493,14 @@ __global__ void __launch_bounds__(kPeelThreads, kBlocksPerSm) k_peel(PeelParams 
     }
 
     // wait limits: level phases (scans, compaction, recount) cover work proportional to the edges;
-    // a round's closing barrier covers the row entries queued for the round (read at its start)
+    // a round's closing barrier covers the round's queued chunks, each of at most 1 << cw_shift row
+    // entries (read at its start; the count includes chunks that overflowed to the block queue)
     const uint64_t phase_wait = P.wait_base_ns + P.wait_ns_per_unit * 2ull * P.m;
-    unsigned long long* round_walk = reinterpret_cast<unsigned long long*>(ctrl + kPRoundWalk);
     for (uint64_t j = tid; j < P.m; j += nthreads) {
         P.rnd[j] = 0;
         P.tr[j] = 0;
     }
-    if (!grid_barrier(ctrl, nblocks, phase_wait)) return;
+    if (!peel_barrier(ctrl, nblocks, phase_wait)) return;
     KT_PHASE(0)
 
     // r: stamp of the last round run.  A level's first round skips one stamp: the blocks still
@@ -482,13 +520,12 @@ __global__ void __launch_bounds__(kPeelThreads, kBlocksPerSm) k_peel(PeelParams 
         }
         if (leader) {
             chunk_ctr[(rr + 1) & 3] = 0;
-            round_walk[(rr + 1) & 3] = 0;
             ctrl[kPBigCount + ((rr + 1) & 3)] = ctrl[kPEdges + ((rr + 1) & 3)] = 0;
         }
         // compact the rows once the alive edges have dropped enough since the last compaction
         if ((uint64_t)live * 100 < (uint64_t)live_at_compaction * compact_num()) {
             compact_rows(P, r, warp_cnt);
-            if (!grid_barrier(ctrl, nblocks, phase_wait)) return;
+            if (!peel_barrier(ctrl, nblocks, phase_wait)) return;
             KT_PHASE(3)
             ++compactions;
             live_at_compaction = live;
@@ -539,25 +576,33 @@ __global__ void __launch_bounds__(kPeelThreads, kBlocksPerSm) k_peel(PeelParams 
             n_alive = __reduce_add_sync(kFullMask, n_alive);
             mn = __reduce_min_sync(kFullMask, mn);
             min_id = __reduce_min_sync(kFullMask, min_id);
-            if (lane == 0) {
-                if (n_alive) atomicAdd(ctrl + kPLAlive + ls, n_alive);
-                if (mn != kDead) atomicMin(ctrl + kPLMin + ls, mn);
-                if (min_id != kDead) atomicMin(ctrl + kPLMinId + ls, min_id);
+            if (lane == 0 && n_alive) {
+                atomicAdd(&s_lv_alive, n_alive);
+                atomicMin(&s_lv_min, mn);
+                atomicMin(&s_lv_min_id, min_id);
             }
-            if (!grid_barrier(ctrl, nblocks, phase_wait)) return;
+            __syncthreads();
+            if (threadIdx.x == 0 && s_lv_alive) {
+                atomicAdd(ctrl + kPLAlive + ls, s_lv_alive);
+                atomicMin(ctrl + kPLMin + ls, s_lv_min);
+                atomicMin(ctrl + kPLMinId + ls, s_lv_min_id);
+                s_lv_alive = 0;
+                s_lv_min = s_lv_min_id = kDead;
+            }
+            if (!peel_barrier(ctrl, nblocks, phase_wait)) return;
             KT_PHASE(1)
             if (ld_acquire(ctrl + kPLAlive + ls) == 0) break;
             k = ld_acquire(ctrl + kPLMin + ls) + 3;
             lvl_start = ld_acquire(ctrl + kPLMinId + ls);
             if (k != kg) {
                 collect(P, k - 3, rr, lvl_start, tid, nthreads);
-                if (!grid_barrier(ctrl, nblocks, phase_wait)) return;
+                if (!peel_barrier(ctrl, nblocks, phase_wait)) return;
                 KT_PHASE(2)
             }
         } else {
             k = P.single_k;
             collect(P, k - 3, rr, 0u, tid, nthreads);
-            if (!grid_barrier(ctrl, nblocks, phase_wait)) return;
+            if (!peel_barrier(ctrl, nblocks, phase_wait)) return;
             KT_PHASE(2)
         }
         const uint32_t km2 = k - 2;
@@ -579,7 +624,6 @@ __global__ void __launch_bounds__(kPeelThreads, kBlocksPerSm) k_peel(PeelParams 
             if (leader) {
                 const uint32_t z = (r + 2) & 3;
                 chunk_ctr[z] = 0;
-                round_walk[z] = 0;
                 ctrl[kPBigCount + z] = 0;
                 ctrl[kPEdges + z] = 0;
                 if (rounds < P.cap_rounds) {
@@ -589,10 +633,11 @@ __global__ void __launch_bounds__(kPeelThreads, kBlocksPerSm) k_peel(PeelParams 
             }
             const bool recount = recount_num() != 0 && (uint64_t)E * 100 >= (uint64_t)recount_num() * live;
             if (leader) phase_ns[8] = phase_ns[6];
-            // limit of the barrier that closes the round: base + the round's queued row entries
+            // limit of the barrier that closes the round: base + the round's queued chunk entries
             const uint64_t round_wait =
                 threadIdx.x == 0 ? (recount ? phase_wait
-                                            : P.wait_base_ns + P.wait_ns_per_unit * ld_acquire_u64(round_walk + (r & 3)))
+                                            : P.wait_base_ns + P.wait_ns_per_unit *
+                                                                   (ld_acquire_u64(chunk_ctr + (r & 3)) << cw_shift()))
                                  : 0;
             if (recount) {
                 // the whole frontier is removed at once (truss number k-1), the support of every
@@ -606,10 +651,10 @@ __global__ void __launch_bounds__(kPeelThreads, kBlocksPerSm) k_peel(PeelParams 
                         P.sup[j] = 0;
                     }
                 }
-                if (!grid_barrier(ctrl, nblocks, phase_wait)) return;
+                if (!peel_barrier(ctrl, nblocks, phase_wait)) return;
                 KT_PHASE(4)
                 recount_support(P, lvl_start, tid, nthreads);
-                if (!grid_barrier(ctrl, nblocks, phase_wait)) return;
+                if (!peel_barrier(ctrl, nblocks, phase_wait)) return;
                 KT_PHASE(4)
                 collect(P, k - 3, r + 1, lvl_start, tid, nthreads);
             } else {
@@ -663,7 +708,7 @@ __global__ void __launch_bounds__(kPeelThreads, kBlocksPerSm) k_peel(PeelParams 
                 }
             }
             }
-            if (!grid_barrier(ctrl, nblocks, round_wait)) return;
+            if (!peel_barrier(ctrl, nblocks, round_wait)) return;
             if (leader && rounds < P.cap_rounds) P.round_ns[rounds] = (uint32_t)(global_ns() - phase_ns[8]);
             KT_PHASE(recount ? 4 : 5)
             live -= E;
@@ -675,6 +720,8 @@ __global__ void __launch_bounds__(kPeelThreads, kBlocksPerSm) k_peel(PeelParams 
         k_last = k;
         if (P.single_k != 0) break;
     }
+    __syncthreads();
+    if (threadIdx.x == 0 && s_walk) atomicAdd(reinterpret_cast<unsigned long long*>(ctrl + kPWalk), s_walk);
     if (leader) {
         ctrl[kPKmax] = P.single_k ? 0 : k_last - 1;
         ctrl[kPRounds] = rounds;
@@ -697,7 +744,7 @@ __global__ void k_barrier_probe(uint32_t* ctrl, uint64_t timeout_ns) {
 
 __global__ void k_init_peel_ctrl(uint32_t* ctrl) {
     const uint32_t i = threadIdx.x;
-    if ((i >= kPBarCount && i < kPSched) || (i >= kPRoundWalk && i < kPRoundWalk + 8))
+    if (i >= kPBarCount && i < kPSched)
         ctrl[i] = (i >= kPLMin && i < kPLMin + 4) || (i >= kPLMinId && i < kPLMinId + 4) ? 0xffffffffu : 0u;
 }
 
@@ -776,9 +823,10 @@ int launch_peel(kt_engine* e, uint32_t single_k) {
     // SM, 342 ms with two)
     const bool wide = e->sched.peel_blocks == 2 ||
                       (e->sched.peel_blocks == 0 && !e->batch_call && 4 * ((uint64_t)e->m + e->n + 1) > (uint64_t)l2);
-    const void* kernel = wide ? (const void*)k_peel<2> : (const void*)k_peel<1>;
+    const void* kernel = wide ? (const void*)k_peel<kWideBlocks> : (const void*)k_peel<1>;
+    const int threads = wide ? kWideThreads : kPeelThreads;
     int per_sm = 0;
-    if ((rc = check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kPeelThreads, 0),
+    if ((rc = check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, 0),
                          "occupancy of k_peel")))
         return rc;
     if (per_sm < 1) return fail(KT_ERR_CUDA, "k_peel cannot be resident (occupancy 0)");
@@ -823,9 +871,9 @@ int launch_peel(kt_engine* e, uint32_t single_k) {
     void* args[] = {&P};
     const bool timed = e->ev_peel0 && e->ev_peel1 && !e->trusted;
     if (timed && (rc = check_cuda(cudaEventRecord(e->ev_peel0, e->stream), "record event"))) return rc;
-    const int blocks_per_sm = wide && per_sm >= 2 ? 2 : 1;
+    const int blocks_per_sm = wide ? std::min(per_sm, kWideBlocks) : 1;
     rc = check_cuda(cudaLaunchCooperativeKernel(kernel, dim3((unsigned)(e->num_sms * blocks_per_sm)),
-                                                dim3(kPeelThreads),
+                                                dim3((unsigned)threads),
                                                 args, 0, e->stream),
                     "cooperative launch of k_peel");
     count_launch(e);

@@ -42,16 +42,22 @@ constexpr int kParams = kB3 + O;
 constexpr int kMean = kParams, kScale = kParams + F, kAll = kParams + 2 * F;
 static_assert(kParams == KT_SELECTOR_PARAMS, "parameter count");
 
-// Forward pass of one sample by a block of H threads; xs: standardized input in shared memory.
+// Forward pass of one sample by the first H threads of a block (all its threads call it: it holds
+// block barriers); xs: standardized input in shared memory.
 __device__ void forward(const float* __restrict__ P, const float* xs, float* h1s, float* h2s, float* os) {
     const int j = threadIdx.x;
-    float a = P[kB1 + j];
-    for (int i = 0; i < F; ++i) a += P[kW1 + j * F + i] * xs[i];
-    h1s[j] = a > 0.f ? a : 0.f;
+    float a;
+    if (j < H) {
+        a = P[kB1 + j];
+        for (int i = 0; i < F; ++i) a += P[kW1 + j * F + i] * xs[i];
+        h1s[j] = a > 0.f ? a : 0.f;
+    }
     __syncthreads();
-    a = P[kB2 + j];
-    for (int i = 0; i < H; ++i) a += P[kW2 + j * H + i] * h1s[i];
-    h2s[j] = a > 0.f ? a : 0.f;
+    if (j < H) {
+        a = P[kB2 + j];
+        for (int i = 0; i < H; ++i) a += P[kW2 + j * H + i] * h1s[i];
+        h2s[j] = a > 0.f ? a : 0.f;
+    }
     __syncthreads();
     if (j < O) {
         a = P[kB3 + j];
@@ -67,6 +73,52 @@ __device__ uint32_t choose(const float* os) {
     for (int v = 1; v < V; ++v)
         if (os[v] > os[best]) best = v;
     return (uint32_t)best * 2u + (os[V] > 0.f ? 1u : 0u);
+}
+
+__device__ __forceinline__ float warp_sum(float a) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(kFullMask, a, o);
+    return a;
+}
+
+// Dense layer for inference, one unit per warp at a time: the lanes read the unit's weight row
+// coalesced (K <= 64 inputs, two per lane) and sum by shuffles; each warp issues the loads of kU
+// units before it reduces any, so the weights cost a few L2 round trips instead of one per input.
+template <int K, int N, bool kRelu>
+__device__ __forceinline__ void infer_layer(const float* __restrict__ W, const float* __restrict__ bias,
+                                            const float* in, float* out) {
+    static_assert(K <= 64, "two inputs per lane");
+    constexpr int kU = 8;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int j0 = warp * kU; j0 < N; j0 += nw * kU) {
+        float a[kU];
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {
+            const int j = j0 + u;
+            a[u] = 0.f;
+            if (j < N) {
+                if (lane < K) a[u] = W[j * K + lane] * in[lane];
+                if (lane + 32 < K) a[u] += W[j * K + lane + 32] * in[lane + 32];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {
+            const float t = warp_sum(a[u]) + (j0 + u < N ? bias[j0 + u] : 0.f);
+            if (lane == 0 && j0 + u < N) out[j0 + u] = kRelu ? (t > 0.f ? t : 0.f) : t;
+        }
+    }
+}
+
+// Forward pass of one sample for inference by all threads of a block (whole warps; it holds block
+// barriers).  Same network as `forward`; the sums run in another order, so logits may differ from
+// it in the last bits.
+__device__ void infer(const float* __restrict__ P, const float* xs, float* h1s, float* h2s, float* os) {
+    infer_layer<F, H, true>(P + kW1, P + kB1, xs, h1s);
+    __syncthreads();
+    infer_layer<H, H, true>(P + kW2, P + kB2, h1s, h2s);
+    __syncthreads();
+    infer_layer<H, O, false>(P + kW3, P + kB3, h2s, os);
+    __syncthreads();
 }
 
 // One block per training sample: forward, loss, and the gradients of the pre-activations
@@ -168,116 +220,123 @@ __global__ void __launch_bounds__(H) k_predict(const float* __restrict__ P, cons
     const uint32_t b = blockIdx.x, j = threadIdx.x;
     if (j < F) xs[j] = (X[(size_t)b * F + j] - P[kMean + j]) / P[kScale + j];
     __syncthreads();
-    forward(P, xs, h1s, h2s, os);
+    infer(P, xs, h1s, h2s, os);
     if (j == 0) choice[b] = choose(os);
 }
 
 // Graph statistics (integers, exact): per vertex (rank space) degree d and oriented out-degree
-// od; per edge the walk length min(d_u, d_v).
+// od; per edge the walk length min(d_u, d_v).  Sums except kMaxD and kMaxOd (maxima).
 enum : int {
-    kSumD2 = 0, kMaxD, kLowD, kHighD, kMaxOd, kSumOd2, kSumMin, kSumMin2, kShortMin, kLongMin, kTicket = 15,
-    kStats = 16
+    kSumD2 = 0, kMaxD, kLowD, kHighD, kMaxOd, kSumOd2, kSumMin, kSumMin2, kShortMin, kLongMin, kNumStat,
+    kTicket = 15, kStats = 16
 };
+constexpr int kSelThreads = 256;                  // statistics block (its first H threads run the network)
+constexpr int kSelWarps = kSelThreads / 32;
+static_assert(kSelThreads >= H && H >= F && H >= O, "the network runs on the first H threads");
 
-__device__ __forceinline__ void vertex_stats(const uint32_t* __restrict__ s_ptr, const uint32_t* __restrict__ o_ptr,
-                                             uint32_t n, unsigned long long* __restrict__ st) {
-    unsigned long long d2 = 0, od2 = 0, low = 0, high = 0;
-    uint32_t maxd = 0, maxod = 0;
-    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
-        const uint32_t d = s_ptr[v + 1] - s_ptr[v], od = o_ptr[v + 1] - o_ptr[v];
-        d2 += (unsigned long long)d * d;
-        od2 += (unsigned long long)od * od;
-        low += d <= 2;
-        high += d >= 64;
-        maxd = max(maxd, d);
-        maxod = max(maxod, od);
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-        d2 += __shfl_xor_sync(kFullMask, d2, o);
-        od2 += __shfl_xor_sync(kFullMask, od2, o);
-        low += __shfl_xor_sync(kFullMask, low, o);
-        high += __shfl_xor_sync(kFullMask, high, o);
-    }
-    maxd = __reduce_max_sync(kFullMask, maxd);
-    maxod = __reduce_max_sync(kFullMask, maxod);
-    if (lane_id() == 0) {
-        atomicAdd(st + kSumD2, d2);
-        atomicAdd(st + kSumOd2, od2);
-        atomicAdd(st + kLowD, low);
-        atomicAdd(st + kHighD, high);
-        atomicMax(st + kMaxD, (unsigned long long)maxd);
-        atomicMax(st + kMaxOd, (unsigned long long)maxod);
-    }
-}
+__device__ __forceinline__ bool stat_is_max(int s) { return s == kMaxD || s == kMaxOd; }
 
-__device__ __forceinline__ void edge_stats(const uint32_t* __restrict__ s_ptr, const uint32_t* __restrict__ e_src,
-                                           const uint32_t* __restrict__ o_col, uint32_t m,
-                                           unsigned long long* __restrict__ st) {
-    unsigned long long s1 = 0, s2 = 0, shrt = 0, lng = 0;
-    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < m; j += gridDim.x * blockDim.x) {
-        const uint32_t u = e_src[j], v = o_col[j];
-        const uint32_t du = s_ptr[u + 1] - s_ptr[u], dv = s_ptr[v + 1] - s_ptr[v];
-        const uint32_t w = min(du, dv);
-        s1 += w;
-        s2 += (unsigned long long)w * w;
-        shrt += w <= 8;
-        lng += w >= 32;
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-        s1 += __shfl_xor_sync(kFullMask, s1, o);
-        s2 += __shfl_xor_sync(kFullMask, s2, o);
-        shrt += __shfl_xor_sync(kFullMask, shrt, o);
-        lng += __shfl_xor_sync(kFullMask, lng, o);
-    }
-    if (lane_id() == 0) {
-        atomicAdd(st + kSumMin, s1);
-        atomicAdd(st + kSumMin2, s2);
-        atomicAdd(st + kShortMin, shrt);
-        atomicAdd(st + kLongMin, lng);
-    }
-}
-
-// Statistics, features and choice in one launch of H-thread blocks: every block adds its share of
-// the vertex and edge statistics; the last block to finish (an atomic ticket in st[kTicket], after a
-// fence) turns them into the 16 features and, with P, runs the network and writes the choice and
-// its schedule.  st must be zero on entry.
-__global__ void __launch_bounds__(H) k_select(const uint32_t* __restrict__ s_ptr, const uint32_t* __restrict__ o_ptr,
-                                              const uint32_t* __restrict__ e_src, const uint32_t* __restrict__ o_col,
-                                              uint32_t n, uint32_t m, unsigned long long* __restrict__ st,
-                                              const float* __restrict__ P, float* __restrict__ feat,
-                                              uint32_t* __restrict__ choice, uint32_t* __restrict__ sched) {
+// Statistics, features and choice in one launch: every block reduces its share of the vertex and
+// edge statistics to one partial per statistic (part[block * kNumStat + s], plain stores - no
+// contended atomics); the last block to finish (an atomic ticket in st[kTicket], after a fence)
+// reduces the partials, turns them into the 16 features and, with P, runs the network and writes
+// the choice and its schedule.  st[kTicket] must be zero on entry; gridDim.x <= kSelMaxBlocks.
+__global__ void __launch_bounds__(kSelThreads) k_select(const uint32_t* __restrict__ s_ptr,
+                                                        const uint32_t* __restrict__ o_ptr,
+                                                        const uint32_t* __restrict__ e_src,
+                                                        const uint32_t* __restrict__ o_col, uint32_t n, uint32_t m,
+                                                        unsigned long long* __restrict__ st,
+                                                        unsigned long long* __restrict__ part,
+                                                        const float* __restrict__ P, float* __restrict__ feat,
+                                                        uint32_t* __restrict__ choice, uint32_t* __restrict__ sched) {
     __shared__ float fs[F], xs[F], h1s[H], h2s[H], os[O];
+    __shared__ unsigned long long ws[kSelWarps][kNumStat], tot[kNumStat];
     __shared__ uint32_t last;
-    vertex_stats(s_ptr, o_ptr, n, st);
-    edge_stats(s_ptr, e_src, o_col, m, st);
-    __threadfence();
+    unsigned long long v[kNumStat] = {};
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t x = blockIdx.x * blockDim.x + threadIdx.x; x < n; x += stride) {
+        const uint32_t d = s_ptr[x + 1] - s_ptr[x], od = o_ptr[x + 1] - o_ptr[x];
+        v[kSumD2] += (unsigned long long)d * d;
+        v[kSumOd2] += (unsigned long long)od * od;
+        v[kLowD] += d <= 2;
+        v[kHighD] += d >= 64;
+        v[kMaxD] = max(v[kMaxD], (unsigned long long)d);
+        v[kMaxOd] = max(v[kMaxOd], (unsigned long long)od);
+    }
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < m; j += stride) {
+        const uint32_t a = e_src[j], b = o_col[j];
+        const uint32_t w = min(s_ptr[a + 1] - s_ptr[a], s_ptr[b + 1] - s_ptr[b]);
+        v[kSumMin] += w;
+        v[kSumMin2] += (unsigned long long)w * w;
+        v[kShortMin] += w <= 8;
+        v[kLongMin] += w >= 32;
+    }
+#pragma unroll
+    for (int q = 0; q < kNumStat; ++q) {
+        for (int o = 16; o > 0; o >>= 1) {
+            const unsigned long long t = __shfl_xor_sync(kFullMask, v[q], o);
+            v[q] = stat_is_max(q) ? max(v[q], t) : v[q] + t;
+        }
+    }
+    const uint32_t warp = threadIdx.x >> 5;
+    if (lane_id() == 0)
+#pragma unroll
+        for (int q = 0; q < kNumStat; ++q) ws[warp][q] = v[q];
+    __syncthreads();
+    if (threadIdx.x < kNumStat) {
+        const int q = threadIdx.x;
+        unsigned long long r = 0;
+        for (int w = 0; w < kSelWarps; ++w) r = stat_is_max(q) ? max(r, ws[w][q]) : r + ws[w][q];
+        part[(size_t)blockIdx.x * kNumStat + q] = r;
+        __threadfence();
+    }
     __syncthreads();
     if (threadIdx.x == 0) last = atomicAdd(st + kTicket, 1ull) == gridDim.x - 1;
     __syncthreads();
     if (!last) return;
     __threadfence();
+    // last block: partials of all blocks, kNumStat groups of kSelThreads / kNumStat threads
+    if (threadIdx.x < kNumStat) tot[threadIdx.x] = 0;
+    __syncthreads();
+    constexpr uint32_t kGroup = kSelThreads / kNumStat;
+    if (threadIdx.x < kGroup * kNumStat) {
+        const int q = threadIdx.x / kGroup;
+        unsigned long long r = 0;
+        for (uint32_t blk = threadIdx.x % kGroup; blk < gridDim.x; blk += kGroup) {
+            const unsigned long long t = __ldcg(part + (size_t)blk * kNumStat + q);
+            r = stat_is_max(q) ? max(r, t) : r + t;
+        }
+        if (stat_is_max(q))
+            atomicMax(&tot[q], r);
+        else
+            atomicAdd(&tot[q], r);
+    }
+    __syncthreads();
     const int j = threadIdx.x;
-    if (j == 0) {
+    if (j == 0) st[kTicket] = 0;  // ready for the next call
+    if (j < F) {  // one feature per thread
         const double dn = n > 0 ? (double)n : 1.0, dm = m > 0 ? (double)m : 1.0;
         const double avg = 2.0 * m / dn;
-        const double var = fmax((double)st[kSumD2] / dn - avg * avg, 0.0);
-        const double od_mean = m / dn;
-        fs[0] = (float)log2(dn);
-        fs[1] = (float)log2(dm + 1.0);
-        fs[2] = (float)avg;
-        fs[3] = (float)log2((double)st[kMaxD] + 1.0);
-        fs[4] = avg > 0 ? (float)(sqrt(var) / avg) : 0.f;
-        fs[5] = (float)log2((double)st[kSumD2] / (2.0 * dm) + 1.0);
-        fs[6] = (float)((double)st[kLowD] / dn);
-        fs[7] = (float)((double)st[kHighD] / dn);
-        fs[8] = (float)log2((double)st[kMaxOd] + 1.0);
-        fs[9] = od_mean > 0 ? (float)(sqrt((double)st[kSumOd2] / dn) / od_mean) : 0.f;
-        fs[10] = (float)log2((double)st[kSumMin] / dm + 1.0);
-        fs[11] = (float)((double)st[kShortMin] / dm);
-        fs[12] = (float)((double)st[kLongMin] / dm);
-        fs[13] = n > 1 ? (float)log2(2.0 * m / (dn * (dn - 1.0)) + 1e-12) : 0.f;
-        fs[14] = (float)log2(sqrt((double)st[kSumMin2] / dm) + 1.0);
-        fs[15] = avg > 0 ? (float)log2((double)st[kMaxD] / avg + 1.0) : 0.f;
+        double f = 0.0;
+        switch (j) {
+            case 0: f = log2(dn); break;
+            case 1: f = log2(dm + 1.0); break;
+            case 2: f = avg; break;
+            case 3: f = log2((double)tot[kMaxD] + 1.0); break;
+            case 4: f = avg > 0 ? sqrt(fmax((double)tot[kSumD2] / dn - avg * avg, 0.0)) / avg : 0.0; break;
+            case 5: f = log2((double)tot[kSumD2] / (2.0 * dm) + 1.0); break;
+            case 6: f = (double)tot[kLowD] / dn; break;
+            case 7: f = (double)tot[kHighD] / dn; break;
+            case 8: f = log2((double)tot[kMaxOd] + 1.0); break;
+            case 9: f = m > 0 ? sqrt((double)tot[kSumOd2] / dn) / (m / dn) : 0.0; break;
+            case 10: f = log2((double)tot[kSumMin] / dm + 1.0); break;
+            case 11: f = (double)tot[kShortMin] / dm; break;
+            case 12: f = (double)tot[kLongMin] / dm; break;
+            case 13: f = n > 1 ? log2(2.0 * m / (dn * (dn - 1.0)) + 1e-12) : 0.0; break;
+            case 14: f = log2(sqrt((double)tot[kSumMin2] / dm) + 1.0); break;
+            default: f = avg > 0 ? log2((double)tot[kMaxD] / avg + 1.0) : 0.0; break;
+        }
+        fs[j] = (float)f;
     }
     __syncthreads();
     if (j < F) {
@@ -286,7 +345,7 @@ __global__ void __launch_bounds__(H) k_select(const uint32_t* __restrict__ s_ptr
     }
     __syncthreads();
     if (!P) return;
-    forward(P, xs, h1s, h2s, os);
+    infer(P, xs, h1s, h2s, os);
     if (j == 0) {
         const uint32_t c = choose(os);
         *choice = c;
@@ -408,15 +467,17 @@ int select_schedule(kt_engine* e) {
 
 int graph_features(kt_engine* e, const float* d_params) {
     unsigned long long* st = reinterpret_cast<unsigned long long*>(e->sel_stats);
-    int rc = check_cuda(cudaMemsetAsync(st, 0, sizeof(unsigned long long) * sel::kStats, e->stream), "clear statistics");
-    if (rc) return rc;
-    // one launch: enough 64-thread blocks to cover the larger of n and m once per thread, at most
-    // 16 per SM
+    // no clearing launch: the ticket is zeroed with the workspace and the last block of every
+    // launch clears it again (a launch either runs all its blocks or, if it fails, none)
+    // one launch: blocks for at least four vertices or edges per thread, at most eight per SM and
+    // kSelMaxBlocks (the partials buffer)
     const uint64_t work = std::max<uint64_t>(e->n, e->m);
+    const uint64_t cap = std::min<uint64_t>((uint64_t)e->num_sms * 8, kSelMaxBlocks);
     const uint32_t blocks =
-        (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((work + sel::H - 1) / sel::H, (uint64_t)e->num_sms * 16));
-    sel::k_select<<<blocks, sel::H, 0, e->stream>>>(e->s_ptr, e->o_ptr, e->e_src, e->o_col, e->n, e->m, st, d_params,
-                                                    e->sel_feat, e->sel_choice, e->ctrl + kPSched);
+        (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((work + 4 * sel::kSelThreads - 1) / (4 * sel::kSelThreads), cap));
+    sel::k_select<<<blocks, sel::kSelThreads, 0, e->stream>>>(
+        e->s_ptr, e->o_ptr, e->e_src, e->o_col, e->n, e->m, st, reinterpret_cast<unsigned long long*>(e->sel_part),
+        d_params, e->sel_feat, e->sel_choice, e->ctrl + kPSched);
     count_launch(e);
     return check_launch(e, "k_select");
 }

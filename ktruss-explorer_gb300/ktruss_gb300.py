@@ -69,7 +69,8 @@ class Stats(ctypes.Structure):
                 ("build_ms", ctypes.c_float), ("support_ms", ctypes.c_float), ("peel_ms", ctypes.c_float),
                 ("compactions", ctypes.c_uint32), ("peel_phase_ms", ctypes.c_float * 6),
                 ("peel_kernel_ms", ctypes.c_float), ("select_ms", ctypes.c_float),
-                ("walk_entries", ctypes.c_uint64), ("copy_in_ms", ctypes.c_float), ("copy_out_ms", ctypes.c_float)]
+                ("walk_entries", ctypes.c_uint64), ("copy_in_ms", ctypes.c_float), ("copy_out_ms", ctypes.c_float),
+                ("emit_ms", ctypes.c_float)]
 
     PHASES = ("init", "level_scan", "collect", "compaction", "mark", "process")
 
@@ -185,9 +186,10 @@ def lib() -> ctypes.CDLL:
         L.kt_get_schedule.argtypes = [ctypes.POINTER(Schedule)]
         L.kt_schedule_grid.argtypes = [ctypes.POINTER(Schedule), ctypes.c_uint32]
         L.kt_schedule_grid.restype = ctypes.c_uint32
-        L.kt_engine_autotune.argtypes = [_VP, _VP, _VP, ctypes.c_uint64, ctypes.c_uint32, ctypes.POINTER(Schedule),
-                                         ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(ctypes.c_float),
-                                         ctypes.POINTER(Schedule)]
+        for f in ("kt_engine_autotune", "kt_engine_autotune_batch"):
+            getattr(L, f).argtypes = [_VP, _VP, _VP, ctypes.c_uint64, ctypes.c_uint32, ctypes.POINTER(Schedule),
+                                      ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(ctypes.c_float),
+                                      ctypes.POINTER(Schedule)]
         for g in ("kt_gen_rmat",):
             getattr(L, g).argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_double, ctypes.c_double,
                                       ctypes.c_double, ctypes.c_uint64, ctypes.POINTER(_Edges)]
@@ -445,16 +447,17 @@ class Engine:
         return s
 
     def autotune(self, d_src: int, d_dst: int, num_entries: int, num_nodes: int, candidates=None,
-                 repeats: int = 1) -> tuple:
+                 repeats: int = 1, batch: bool = False) -> tuple:
         """Times every candidate schedule (default: the built-in grid) on this device graph and
-        keeps the fastest; returns (best Schedule, [(Schedule, ms), ...])."""
+        keeps the fastest; returns (best Schedule, [(Schedule, ms), ...]).  batch=True times the
+        candidates as decompose_batch runs them (the graph is the union of a sample batch)."""
         cands = list(candidates) if candidates is not None else schedule_grid()
         arr = (Schedule * len(cands))(*[Schedule(*c.as_tuple()) if isinstance(c, Schedule) else Schedule(*c)
                                         for c in cands])
         ms = (ctypes.c_float * len(cands))()
         best = Schedule()
-        _check(lib().kt_engine_autotune(self._h, d_src, d_dst, num_entries, num_nodes, arr, len(cands), repeats, ms,
-                                        ctypes.byref(best)))
+        fn = lib().kt_engine_autotune_batch if batch else lib().kt_engine_autotune
+        _check(fn(self._h, d_src, d_dst, num_entries, num_nodes, arr, len(cands), repeats, ms, ctypes.byref(best)))
         return best, [(arr[i], ms[i]) for i in range(len(cands))]
 
     def features(self, d_src: int, d_dst: int, num_entries: int, num_nodes: int) -> np.ndarray:

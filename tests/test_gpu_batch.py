@@ -88,3 +88,32 @@ def test_batch_rejects_cross_graph_entries():
     with pytest.raises(kt.KtrussError) as ei:
         kt.decompose_batch(src, dst, 4, np.array([0, 2, 4], np.uint32))
     assert ei.value.status == 1
+
+
+def test_batch_autotuner_keeps_a_schedule_that_decomposes_the_batch():
+    """kt_engine_autotune_batch times candidates as batch decompositions of a sample batch; the
+    schedule it keeps decomposes another batch of the distribution exactly."""
+    torch = pytest.importorskip("torch")
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a, np.uint32).view(np.int32)).cuda()
+    ns, us, vs, _ = kt.gen_batch(24, 300, 2000, 41)
+    ss, sd = both_directions(us, vs)
+    eng = kt.Engine(0)
+    cands = [(4, 8, 0, 50, 0), (8, 16, 85, 0, 0), (16, 32, 0, 0, 0)]
+    d_ss, d_sd = t(ss), t(sd)
+    torch.cuda.synchronize()
+    best, table = eng.autotune(d_ss.data_ptr(), d_sd.data_ptr(), len(ss), ns, candidates=cands, repeats=2, batch=True)
+    assert best.as_tuple() in cands and len(table) == 3 and all(ms > 0 for _, ms in table)
+    assert best.as_tuple() == min(table, key=lambda x: x[1])[0].as_tuple()
+    assert eng.schedule().as_tuple() == best.as_tuple()
+    n, u, v, off = kt.gen_batch(20, 300, 2000, 42)
+    src, dst = both_directions(u, v)
+    d_src, d_dst, d_off = t(src), t(dst), t(off)
+    d_out = torch.zeros(len(src), dtype=torch.int32, device="cuda")
+    d_k = torch.zeros(len(off) - 1, dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    eng.decompose_batch(d_src.data_ptr(), d_dst.data_ptr(), len(src), n, d_off.data_ptr(), len(off) - 1,
+                        d_out.data_ptr(), d_k.data_ptr())
+    truss, kmax = _per_graph_oracle(n, u, v, off)
+    assert np.array_equal(d_out.cpu().numpy().view(np.uint32)[: len(u)], truss)
+    assert np.array_equal(d_k.cpu().numpy().view(np.uint32), kmax)
+    eng.close()

@@ -92,6 +92,11 @@ def test_engine_stats_match_reference_pass_accounting():
     assert s.plain_alive_sum == ref["plain_alive_sum"]
     assert s.num_rounds == ref["rounds"]
     assert s.num_edges == len(u)
+    # the per-entry output is timed inside the peel phase; single-k calls do not time it
+    assert 0 < s.emit_ms <= s.peel_ms
+    d_keep = torch.zeros(len(src), dtype=torch.uint8, device="cuda")
+    eng.ktruss(d_src.data_ptr(), d_dst.data_ptr(), len(src), n, 4, d_keep.data_ptr())
+    assert eng.stats().emit_ms == 0
     eng.close()
 
 

@@ -90,7 +90,10 @@ def _features_numpy(n, u, v):
 
 
 @pytest.mark.parametrize("make", [lambda: kt.gen_rmat(12, 16, 0.57, 0.19, 0.19, 3),
-                                  lambda: kt.plant_cliques(*kt.gen_ba(3000, 4, 4), 2, 30, 70, 5)])
+                                  lambda: kt.plant_cliques(*kt.gen_ba(3000, 4, 4), 2, 30, 70, 5),
+                                  # one statistics block; the most blocks, several items per thread
+                                  lambda: kt.gen_er(60, 0.2, 7),
+                                  lambda: kt.gen_rmat(18, 16, 0.57, 0.19, 0.19, 5)])
 def test_features_match_definition(make):
     torch = pytest.importorskip("torch")
     n, u, v = make()
