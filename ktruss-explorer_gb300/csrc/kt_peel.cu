@@ -769,29 +769,47 @@ __global__ void k_emit_keep(const uint32_t* __restrict__ entry_eid, uint64_t ent
 
 __global__ void k_copy_u32(uint32_t* dst, const uint32_t* src) { *dst = *src; }
 
+// Graph of vertex s: the last g with offsets[g] <= s (num_graphs when s is past the last range,
+// 0xffffffff when it is below the first).
+__device__ __forceinline__ uint32_t graph_of(const uint32_t* __restrict__ offsets, uint32_t num_graphs, uint32_t s) {
+    uint32_t lo = 0, len = num_graphs + 1;
+    while (len > 0) {
+        const uint32_t half = len >> 1;
+        if (offsets[lo + half] <= s) {
+            lo += half + 1;
+            len -= half + 1;
+        } else {
+            len = half;
+        }
+    }
+    return lo - 1;
+}
+
 // Per-graph k_max of a batch: entry i belongs to the graph whose vertex range holds its source;
 // lanes of a warp with the same graph combine before the atomic.  An entry whose endpoints lie in
-// different graphs sets kErrCrossGraph.
+// different graphs sets kErrCrossGraph.  Batches usually list their graphs one after another, so
+// the warp first searches the graph of its first active lane's source and a lane searches on its
+// own only when its source lies outside that graph's range.
 __global__ void k_graph_kmax(const uint32_t* __restrict__ src, const uint32_t* __restrict__ dst, uint64_t entries,
                              const uint32_t* __restrict__ offsets, uint32_t num_graphs,
                              const uint32_t* __restrict__ truss, uint32_t* __restrict__ kmax,
                              uint32_t* __restrict__ ctrl) {
     const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    uint32_t g = 0xffffffffu, t = 0, err = 0;
-    if (i < entries) {
-        const uint32_t s = src[i], d = dst[i];
-        // graph of s: last g with offsets[g] <= s
-        uint32_t lo = 0, len = num_graphs + 1;
-        while (len > 0) {
-            const uint32_t half = len >> 1;
-            if (offsets[lo + half] <= s) {
-                lo += half + 1;
-                len -= half + 1;
-            } else {
-                len = half;
-            }
+    const bool active = i < entries;
+    const uint32_t s = active ? src[i] : 0u, d = active ? dst[i] : 0u;
+    const uint32_t act = __ballot_sync(kFullMask, active);
+    uint32_t g0 = 0xffffffffu, lo0 = 1u, hi0 = 0u;  // an empty range when the warp has no entry
+    if (act) {
+        const uint32_t s0 = __shfl_sync(kFullMask, s, __ffs(act) - 1);
+        g0 = graph_of(offsets, num_graphs, s0);  // the same address in every lane
+        if (g0 < num_graphs) {
+            lo0 = offsets[g0];
+            hi0 = offsets[g0 + 1];
         }
-        g = lo - 1;
+    }
+    uint32_t g = 0xffffffffu, t = 0, err = 0;
+    if (active) {
+        g = s >= lo0 && s < hi0 ? g0 : graph_of(offsets, num_graphs, s);
         if (g >= num_graphs || d < offsets[g] || d >= offsets[g + 1]) {
             err = kErrCrossGraph;
             g = 0xffffffffu;

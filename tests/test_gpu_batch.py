@@ -117,3 +117,25 @@ def test_batch_autotuner_keeps_a_schedule_that_decomposes_the_batch():
     assert np.array_equal(d_out.cpu().numpy().view(np.uint32)[: len(u)], truss)
     assert np.array_equal(d_k.cpu().numpy().view(np.uint32), kmax)
     eng.close()
+
+
+def test_batch_kmax_with_entries_in_any_order():
+    """Per-graph k_max does not depend on the entries being listed graph by graph (a warp's entries
+    then span many graphs), and a cross-graph entry among one graph's entries is still found."""
+    n, u, v, off = kt.gen_batch(40, 64, 800, 9)
+    src, dst = both_directions(u, v)
+    truss, kmax = kt.decompose_batch(src, dst, n, off)
+    perm = np.random.default_rng(3).permutation(len(src))
+    truss_p, kmax_p = kt.decompose_batch(src[perm], dst[perm], n, off)
+    assert np.array_equal(kmax_p, kmax)
+    assert np.array_equal(truss_p, truss[perm])
+    # two 12-cliques; one entry pair joins them, placed among the first clique's entries
+    iu, iv = np.triu_indices(12, 1)
+    cu = np.concatenate([iu, iu + 12]).astype(np.uint32)
+    cv = np.concatenate([iv, iv + 12]).astype(np.uint32)
+    s2, d2 = both_directions(cu, cv)
+    s2 = np.insert(s2, 40, [3, 15]).astype(np.uint32)
+    d2 = np.insert(d2, 40, [15, 3]).astype(np.uint32)
+    with pytest.raises(kt.KtrussError) as ei:
+        kt.decompose_batch(s2, d2, 24, np.array([0, 12, 24], np.uint32))
+    assert ei.value.status == 1
