@@ -444,8 +444,9 @@ __device__ __forceinline__ void collect(const PeelParams& P, uint32_t thr, uint3
 
 // Two builds of the kernel: one block per SM (64 registers a thread) for graphs whose oriented
 // CSR fits in L2, and two blocks per SM (32 registers, twice the warps to hide DRAM latency) for
-// larger graphs, whose walks wait on DRAM.  Measured on GB300: R-MAT 20 (CSR in L2) 89 ms with one
-// block and 99 ms with two; R-MAT 24 (CSR 2 GB) 8.65 s with one and 8.21 s with two.
+// larger graphs, whose walks wait on DRAM.  Measured on GB300, peel with one / two blocks per SM:
+// R-MAT 20 (CSR in L2) 65.5 / 67.4 ms, R-MAT 21 (just over L2) 135.0 / 131.4 ms, R-MAT 24 (CSR
+// 2 GB) 6.27 / 4.78 s.
 template <int kBlocksPerSm>
 __global__ void __launch_bounds__(peel_threads<kBlocksPerSm>(), kBlocksPerSm) k_peel(PeelParams P) {
     __shared__ uint32_t warp_cnt[peel_threads<kBlocksPerSm>() / 32];
