@@ -814,7 +814,6 @@ int kt_decompose_batch(const uint32_t* src, const uint32_t* dst, uint64_t num_en
     const size_t need = 2 * (size_t)num_graphs + 1;
     if (e->aux_words < need) {
         if (e->aux) cudaFree(e->aux);
-    if (e->tile_off) cudaFree(e->tile_off);
         e->aux = nullptr;
         e->aux_words = 0;
         if ((rc = check_cuda(cudaMalloc(&e->aux, sizeof(uint32_t) * need), "allocate batch staging"))) return rc;

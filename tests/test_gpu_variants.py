@@ -99,3 +99,22 @@ def test_variant_repeat_runs_replay_directly(torch):
         assert torch.equal(d_keep, first), (d, f)
         assert eng.replay_mode() == ("cuda graph" if d == "directed-by-index" else "direct launches"), (d, f)
     eng.close()
+
+
+def test_tiled_calls_around_a_batch_that_grows_the_default_engine_staging():
+    """The host-buffer calls share one engine: a tiled single-k call (its tile table), a batch call
+    with more graphs than any before it (its staging grows), and the tiled call again, which must
+    still find its own table and the same truss."""
+    n, u, v = kt.gen_rmat(11, 12, 0.57, 0.19, 0.19, 41)
+    g = kt.COOGraph.from_undirected(n, u, v)
+    cfg = kt.Config(k=5, input_format="tiled-coocsr", num_tiles=4, num_parallel_tiles=2)
+    first = kt.ktruss(g, cfg).canonical()
+    # more graphs than any other test's batch, so that the staging grows whatever ran before
+    bn, bu, bv, off = kt.gen_batch(5000, 64, 128, 43)
+    bs, bd = both_directions(bu, bv)
+    truss, kmax = kt.decompose_batch(bs, bd, bn, off)
+    assert len(kmax) == 5000
+    again = kt.ktruss(g, cfg).canonical()
+    assert np.array_equal(first, again)
+    os_, od = oracle.ktruss(n, g.src_idx, g.dst_idx, 5)
+    assert np.array_equal(first, edge_keys(os_, od))
