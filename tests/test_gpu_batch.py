@@ -139,3 +139,25 @@ def test_batch_kmax_with_entries_in_any_order():
     with pytest.raises(kt.KtrussError) as ei:
         kt.decompose_batch(s2, d2, 24, np.array([0, 12, 24], np.uint32))
     assert ei.value.status == 1
+
+
+def test_batch_kmax_of_many_tiny_graphs():
+    """Hundreds of graphs of 6-30 entries each, so that every 32-entry step of a warp spans several
+    graphs: each clique K_s is its own graph with k_max s (K_2 and K_1 give 2 and 0)."""
+    rng = np.random.default_rng(12)
+    sizes = rng.integers(1, 7, 400)
+    us, vs, off = [], [], [0]
+    for s in sizes:
+        iu, iv = np.triu_indices(int(s), 1)
+        us.append(iu + off[-1])
+        vs.append(iv + off[-1])
+        off.append(off[-1] + int(s))
+    u = np.concatenate(us).astype(np.uint32)
+    v = np.concatenate(vs).astype(np.uint32)
+    off = np.array(off, np.uint32)
+    src, dst = both_directions(u, v)
+    truss, kmax = kt.decompose_batch(src, dst, int(off[-1]), off)
+    want = np.where(sizes >= 2, sizes, 0)
+    assert np.array_equal(kmax, want.astype(np.uint32))
+    g = np.searchsorted(off, u, side="right") - 1
+    assert np.array_equal(truss[: len(u)], sizes[g].astype(np.uint32))
