@@ -9,8 +9,8 @@ SplitMix64 counters, the same on x86-64 and AArch64; the oracle has no clique pl
 pinned by its hash.  Every truss number comes from the oracle's exact peel on host threads
 (ko_decompose_peel_mt, the same rounds as its one-thread peel, which the R-MAT 20 fixture
 cross-checks against the chained single-k algorithm of kernel_hdc.cu), with the pass statistics
-of the reference's chained schedule per level.  512.7 M edges: about 40 GB of host memory and an
-hour or more on eight cores.  The fixture keeps hashes and counts only:
+of the reference's chained schedule per level.  512.7 M edges: about 27 GB of host memory and 55
+minutes on eight x86-64 cores.  The fixture keeps hashes and counts only:
   edges_sha256   SHA-256 of the edge list in generator order (u, v pairs), uint32 little-endian
   truss_sha256   SHA-256 of the truss numbers in that order, uint32 little-endian
   histogram      truss number -> edge count
