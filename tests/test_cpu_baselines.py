@@ -30,6 +30,22 @@ def test_batch_processes_match_the_oracle_per_graph():
         assert sha == hashlib.sha256(r["truss"][: len(lu)].astype("<u4").tobytes()).hexdigest(), g
 
 
+def test_peel_processes_on_graphs_in_generator_order():
+    """The held-out set's CPU leg: graphs listed one after another with their edges in generator
+    order (not canonical), decomposed by the exact peel, one process per graph; the same k_max and
+    truss hashes as the chain."""
+    parts = [kt.gen_rmat(9, 8, 0.57, 0.19, 0.19, 3), kt.gen_ba(700, 4, 5), kt.gen_ws(500, 10, 0.1, 6)]
+    us, vs, off = [], [], [0]
+    for n, u, v in parts:
+        us.append(v.astype(np.uint64) + off[-1])  # (v, u): sources not sorted within a graph
+        vs.append(u.astype(np.uint64) + off[-1])
+        off.append(off[-1] + n)
+    u, v, off = np.concatenate(us), np.concatenate(vs), np.array(off, np.uint32)
+    peel, _, _ = oracle.decompose_batch_processes(u, v, off, workers=2, per_task=1, method="peel")
+    chain, _, _ = oracle.decompose_batch_processes(u, v, off, workers=2, per_task=1, method="chain")
+    assert sorted(peel) == sorted(chain) and len(peel) == 3
+
+
 @pytest.mark.parametrize("k", [3, 5, 9])
 def test_threaded_repeat_runs_equal_the_serial_loop(k):
     n, u, v = oracle.gen_rmat(12, 16, 0.57, 0.19, 0.19, 4)
